@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""Benchmark of draw_lines on the detector-stack workload (64 frames of 2167x2070
+float32, Poisson(2,000) segments per frame, gaussian profile, max overlap, int32 frame
+indices): one step = one draw_lines call over the whole stack.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput in Mlines/s
+(lines, indices and frames already in HBM); `e2e` is the same metric through the
+public API with pinned host buffers (frames, lines and indices copied in, frames
+copied out every step).  `roofline` is the render kernel's achieved HBM bandwidth
+from CUDA events recorded on its stream around every launch in the timed region,
+with the read-modify-write byte count 2*F*H*W*4 + N*24 per launch.  `cpu_baseline`
+times the oracle (C port of the reference CPU rasteriser) on a bounded sample with
+all host threads.  Under torchrun each rank renders its own stack (weak scaling, no
+collective on the data path).  `--impl reference` times the reference CPU algorithm
+(the oracle port; the reference sources are not on the GPU host) instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+KERNELS_PER_CALL = 5          # init_status, prep, offsets, fill, render
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=20)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    p.add_argument('--frames', type=int, default=64)
+    p.add_argument('--cpu-frames', type=int, default=8,
+                   help='frames in the bounded CPU-baseline sample')
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--no-e2e', action='store_true')
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
+                 '-lms', '200', '-i', str(self.gpu)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': max(smax) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, 'fallback'
+
+
+def committed_traffic(workload: str):
+    """DRAM bytes per render launch from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, 'profiles', 'render_traffic.json')
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return d.get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(ls, n_frames: int, repeats: int = 3):
+    """The oracle (reference CPU algorithm, C port) on the first frames, all threads."""
+    import oracle
+    from cbclib_v2_gb300 import workloads
+    sub = workloads.frames_subset(ls, list(range(min(n_frames, ls.shape[0]))))
+    lines = sub.lines.astype(np.float32)
+    threads = len(os.sched_getaffinity(0))
+    best = float('inf')
+    for _ in range(repeats):
+        out = np.zeros(sub.shape, np.float32)
+        t0 = time.perf_counter()
+        oracle.draw_lines(out, lines, sub.idxs, sub.max_val, sub.kernel, sub.overlap, threads)
+        best = min(best, time.perf_counter() - t0)
+    return {'value': sub.n_lines / best / 1e6, 'unit': 'Mlines/s', 'cores': threads,
+            'kind': 'port', 'seconds': best,
+            'sample': f'{sub.shape[0]} of {ls.shape[0]} frames ({sub.n_lines} lines), '
+                      f'best of {repeats}'}
+
+
+def run_reference(args, ls, world, rank):
+    if rank != 0:
+        return
+    import oracle  # noqa: F401  (builds the C port on first use)
+    cfg = workload_config(ls)
+    for _ in range(args.warmup):
+        cpu_baseline(ls, 2, repeats=1)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(ls, args.cpu_frames, repeats=1))
+    secs = sum(v['seconds'] for v in vals)
+    lines = sum(float(v['sample'].split('(')[1].split()[0]) for v in vals)
+    value = lines / secs / 1e6
+    cb = dict(vals[0])
+    cb['value'] = value
+    cb['sample'] = f'{args.cpu_frames} of {ls.shape[0]} frames per step'
+    cb.pop('seconds', None)
+    print(json.dumps({
+        'impl': 'reference', 'metric': 'draw_lines throughput', 'value': value,
+        'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': secs / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic', 'config': cfg,
+        'cpu_baseline': cb,
+        'e2e': {'value': value, 'unit': 'Mlines/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0}}), flush=True)
+
+
+def workload_config(ls):
+    F, H, W = ls.shape
+    return {'workload': ls.name, 'frames': F, 'height': H, 'width': W, 'lines': ls.n_lines,
+            'kernel': ls.kernel, 'overlap': ls.overlap, 'idx_dtype': 'int32',
+            'out_dtype': 'float32', 'contract': 'read-modify-write of out',
+            'l2': 'output frames (%.2f GB) exceed L2; no flush' % (F * H * W * 4 / 1e9)}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    import torch
+    from cbclib_v2_gb300 import _native, draw_lines, workloads
+
+    ls = workloads.detector_stack(seed=1000 + rank, F=args.frames)
+    if args.impl == 'reference':
+        run_reference(args, ls, world, rank)
+        return
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', init_method='env://')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    F, H, W = ls.shape
+    N = ls.n_lines
+    lines = torch.from_numpy(ls.lines.astype(np.float32)).to(dev)
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)
+    out = torch.zeros(ls.shape, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier(device_ids=[local])
+
+    for _ in range(args.warmup):
+        draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    _native.profile_enable(True)
+    _native.profile_read(reset=True)
+    barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    prof = _native.profile_read(reset=True)
+    _native.profile_enable(False)
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1)
+    if dist is not None:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_step = ms / args.steps
+    value = world * N / (ms_step * 1e-3) / 1e6
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_out = torch.zeros(ls.shape, dtype=torch.float32).pin_memory()
+        h_lines = torch.from_numpy(ls.lines.astype(np.float32)).pin_memory()
+        h_idxs = torch.from_numpy(ls.idxs.astype(np.int32)).pin_memory()
+        for _ in range(max(1, args.warmup)):
+            draw_lines(h_out, h_lines, h_idxs, ls.max_val, ls.kernel, ls.overlap)
+        e_steps = max(3, args.steps // 4)
+        barrier()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e_steps):
+            draw_lines(h_out, h_lines, h_idxs, ls.max_val, ls.kernel, ls.overlap)
+        b.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e_ms = a.elapsed_time(b) / e_steps
+        if dist is not None:
+            tt = torch.tensor([e_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e_ms = float(tt.item())
+        e2e = {'value': world * N / (e_ms * 1e-3) / 1e6, 'unit': 'Mlines/s',
+               'ms_per_step': e_ms,
+               'h2d_bytes_per_step': int(h_out.numel() * 4 + h_lines.numel() * 4 + h_idxs.numel() * 4),
+               'd2h_bytes_per_step': int(h_out.numel() * 4)}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_src = measured_peak()
+    render_ms = prof.ms_render / max(prof.calls, 1)
+    algo_bytes = 2 * F * H * W * 4 + N * 24
+    achieved = algo_bytes / (render_ms * 1e-3) / 1e9
+    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                'frac': achieved / peak, 'peak_source': peak_src,
+                'traffic': committed_traffic(ls.name), 'kernel': 'render_kernel',
+                'algorithmic_bytes': algo_bytes, 'ms_per_launch': render_ms,
+                'stage_ms_per_call': {
+                    'prep': prof.ms_prep / max(prof.calls, 1),
+                    'offsets': prof.ms_offsets / max(prof.calls, 1),
+                    'fill': prof.ms_fill / max(prof.calls, 1),
+                    'render': render_ms}}
+    res = {
+        'metric': 'draw_lines throughput', 'value': value, 'unit': 'Mlines/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic', 'config': workload_config(ls), 'roofline': roofline,
+        'output_gbs': F * H * W * 4 / (ms_step * 1e-3) / 1e9, 'clocks': clk,
+        'gpu_launches': KERNELS_PER_CALL * args.steps, 'e2e': e2e,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        res['cpu_baseline'] = cpu_baseline(ls, args.cpu_frames)
+    print(json.dumps(res), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,108 @@
+"""ctypes binding of the C ABI in include/cbc_draw_lines.h (libcbc_gb300.so).
+
+The library is the only compute path of this package: when it cannot be loaded the
+package raises instead of falling back to anything else.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+CBC_OK, CBC_ERR_INVALID, CBC_ERR_INDEX, CBC_ERR_CAPACITY, CBC_ERR_CUDA, CBC_ERR_RANGE = range(6)
+MAX_WALK = 1 << 22
+
+KERNELS = {'biweight': 0, 'gaussian': 1, 'parabolic': 2, 'rectangular': 3, 'triangular': 4}
+OVERLAPS = {'sum': 0, 'max': 1}
+
+
+class Tuning(ctypes.Structure):
+    """cbc_tuning: render tile shape and lines per shared-memory chunk (0 = default)."""
+    _fields_ = [('tile_w', ctypes.c_int32), ('tile_h', ctypes.c_int32),
+                ('chunk_lines', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+
+
+class Status(ctypes.Structure):
+    """cbc_status: device-side result flags of the last call on a workspace."""
+    _fields_ = [('flags', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('bad_line', ctypes.c_int64), ('idx_min', ctypes.c_int64),
+                ('idx_max', ctypes.c_int64), ('pairs_needed', ctypes.c_int64)]
+
+    def has(self, code: int) -> bool:
+        return bool(self.flags & (1 << code))
+
+
+class Profile(ctypes.Structure):
+    """cbc_profile: accumulated per-stage device milliseconds of profiled calls."""
+    _fields_ = [('calls', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('ms_prep', ctypes.c_double), ('ms_offsets', ctypes.c_double),
+                ('ms_fill', ctypes.c_double), ('ms_render', ctypes.c_double)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+# every symbol declared in include/cbc_draw_lines.h
+EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_lines_f64',
+           'cbc_read_status', 'cbc_profile_enable', 'cbc_profile_read', 'cbc_last_error',
+           'cbc_version')
+
+
+def _declare(lib):
+    p, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+    lib.cbc_draw_lines_workspace_size.argtypes = [i64, i64, i64, i64, i64, i32,
+                                                  ctypes.POINTER(Tuning)]
+    lib.cbc_draw_lines_workspace_size.restype = ctypes.c_size_t
+    for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
+        f = getattr(lib, 'cbc_draw_lines_' + sfx)
+        f.argtypes = [p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, ctypes.c_size_t,
+                      i64, ctypes.POINTER(Tuning), p]
+        f.restype = ctypes.c_int
+    lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
+    lib.cbc_read_status.restype = ctypes.c_int
+    lib.cbc_profile_enable.argtypes = [i32]
+    lib.cbc_profile_enable.restype = ctypes.c_int
+    lib.cbc_profile_read.argtypes = [ctypes.POINTER(Profile), i32]
+    lib.cbc_profile_read.restype = ctypes.c_int
+    lib.cbc_last_error.argtypes = []
+    lib.cbc_last_error.restype = ctypes.c_char_p
+    lib.cbc_version.argtypes = []
+    lib.cbc_version.restype = ctypes.c_char_p
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load (building first if the sources are newer) and return the native library."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                path = _build.build()
+                if not os.path.exists(path):
+                    raise RuntimeError(f"native library {path} is missing")
+                handle = ctypes.CDLL(path)
+                _declare(handle)
+                _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().cbc_last_error()
+    return msg.decode() if msg else ''
+
+
+def profile_enable(on: bool) -> bool:
+    """Switch the per-stage CUDA-event timing of the library on or off."""
+    return bool(lib().cbc_profile_enable(1 if on else 0))
+
+
+def profile_read(reset: bool = True) -> Profile:
+    """Accumulated per-stage device times of the profiled calls (waits for them)."""
+    p = Profile()
+    rc = lib().cbc_profile_read(p, 1 if reset else 0)
+    if rc:
+        raise RuntimeError(f"cbc_profile_read failed: {last_error()}")
+    return p

@@ -1,0 +1,209 @@
+"""Drop-in ``cbclib_v2.ndimage.draw_lines`` on the GB300 kernels.
+
+Same signature, argument meaning and error behaviour as the reference's public op
+(cbclib_v2/_src/functions.py:275-302, pybind11 binding bresenham.cpp:329-330):
+``out`` is updated in place and returned.  Results are those of the reference CPU
+path bit for bit (max overlap, and sum apart from the order in which several lines'
+contributions to one pixel are added).
+"""
+import math
+import threading
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _native
+from . import device as _device
+
+__all__ = ['draw_lines', 'Workspace']
+
+
+class Workspace:
+    """Device scratch of one (device, stream, thread): grows on demand, reused by calls.
+
+    Layout and size come from ``cbc_draw_lines_workspace_size``; the pair capacity grows
+    when a call reports that its (line, tile) pairs did not fit."""
+
+    def __init__(self, dev: torch.device):
+        self.device = dev
+        self.buffer: Optional[torch.Tensor] = None
+        self.capacity = 0
+
+    def ensure(self, nbytes: int) -> torch.Tensor:
+        if self.buffer is None or self.buffer.numel() < nbytes:
+            self.buffer = torch.empty(int(nbytes * 1.1) + 4096, dtype=torch.uint8,
+                                      device=self.device)
+        return self.buffer
+
+
+_ws_lock = threading.Lock()
+_workspaces = {}
+
+
+def _workspace(dev: torch.device, stream: torch.cuda.Stream) -> Workspace:
+    key = (dev.index, stream.cuda_stream, threading.get_ident())
+    with _ws_lock:
+        ws = _workspaces.get(key)
+        if ws is None:
+            ws = _workspaces[key] = Workspace(dev)
+        return ws
+
+
+def _check_names(kernel: str, overlap: str) -> Tuple[int, int]:
+    if kernel not in _native.KERNELS:
+        raise ValueError(f"kernel is missing for {kernel}")
+    if overlap not in _native.OVERLAPS:
+        raise ValueError(f"Invalid overlap keyword: {overlap}")
+    return _native.KERNELS[kernel], _native.OVERLAPS[overlap]
+
+
+def _as_device_lines(lines, dev: torch.device, dtype: torch.dtype) -> torch.Tensor:
+    t = torch.as_tensor(lines)
+    if t.ndim < 1:
+        raise ValueError("lines must have at least one dimension")
+    L = t.shape[-1]
+    if L not in (5, 7):
+        raise RuntimeError(f"Invalid lines size ({L}) at axis {t.ndim - 1}")
+    if L == 7:
+        raise NotImplementedError("3-D lines are not supported by the GPU path yet")
+    return t.to(device=dev, dtype=dtype).reshape(-1, L).contiguous()
+
+
+def _as_device_idxs(idxs, n_lines: int, dev: torch.device) -> Optional[torch.Tensor]:
+    if idxs is None:
+        return None
+    t = torch.as_tensor(idxs)
+    if t.is_floating_point() or t.is_complex() or t.dtype == torch.bool:
+        raise TypeError("idxs must be an integer array")
+    t = t.reshape(-1)
+    if t.numel() != n_lines:
+        raise ValueError(f"idxs has an invalid size ({t.numel()} != {n_lines})")
+    if t.dtype not in (torch.int32, torch.int64):
+        t = t.to(torch.int64)
+    return t.to(device=dev).contiguous()
+
+
+def _raise_status(st: _native.Status, n_frames: int):
+    if st.has(_native.CBC_ERR_INDEX):
+        raise IndexError(f"idxs range ({st.idx_min}, {st.idx_max}) is outside of "
+                         f"(0, {n_frames})")
+    if st.has(_native.CBC_ERR_RANGE):
+        raise ValueError(f"line {st.bad_line}: its walk is longer than {_native.MAX_WALK} "
+                         "pixels or its coordinates exceed 2^30")
+
+
+def _raise_rc(rc: int):
+    msg = _native.last_error()
+    if rc == _native.CBC_ERR_INVALID:
+        raise ValueError(msg)
+    raise RuntimeError(f"cbc_draw_lines failed ({rc}): {msg}")
+
+
+def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int,
+                     overlap: int, tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
+    if out.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"out must be float32 or float64, got {out.dtype}")
+    if out.dim() < 2:
+        raise ValueError("Output array has insufficient number of dimensions")
+    dev = out.device
+    ln = _as_device_lines(lines, dev, out.dtype)
+    n_lines = ln.shape[0]
+    ix = _as_device_idxs(idxs, n_lines, dev)
+    H, W = int(out.shape[-2]), int(out.shape[-1])
+    F = math.prod(int(s) for s in out.shape[:-2])
+    if ix is None and n_lines and F != 1 and F != n_lines:
+        raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
+    work = out if out.is_contiguous() else out.contiguous()
+    lib = _native.lib()
+    elem = 4 if out.dtype == torch.float32 else 8
+    fn = lib.cbc_draw_lines_f32 if elem == 4 else lib.cbc_draw_lines_f64
+    with torch.cuda.device(dev):
+        stream = torch.cuda.current_stream(dev)
+        ws = _workspace(dev, stream)
+        capacity = max(ws.capacity, 4 * n_lines + 1024)
+        tref = None if tuning is None else ctypes_pointer(tuning)
+        for _ in range(4):
+            nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity, elem, tref)
+            if nbytes == 0:
+                raise ValueError(_native.last_error() or "invalid sizes or tuning")
+            buf = ws.ensure(nbytes)
+            rc = fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines,
+                    None if ix is None else ix.data_ptr(),
+                    0 if ix is None else ix.element_size(), max_val, kernel, overlap,
+                    buf.data_ptr(), buf.numel(), capacity, tref, stream.cuda_stream)
+            if rc:
+                _raise_rc(rc)
+            st = _native.Status()
+            rc = lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream)
+            if rc:
+                _raise_rc(rc)
+            _raise_status(st, F)
+            if not st.has(_native.CBC_ERR_CAPACITY):
+                ws.capacity = capacity
+                break
+            capacity = int(st.pairs_needed * 1.25) + 1024
+            if capacity > 2**31 - 1:
+                raise MemoryError("too many (line, tile) pairs for one call")
+        else:
+            raise RuntimeError("pair capacity did not converge")
+    if work is not out:
+        out.copy_(work)
+    return out
+
+
+def ctypes_pointer(t: _native.Tuning):
+    import ctypes
+    return ctypes.pointer(t)
+
+
+def draw_lines(out, lines, idxs=None, max_val: float = 1.0, kernel: str = 'rectangular',
+               overlap: str = 'sum'):
+    """Draw thick lines with variable thickness and antialiasing into ``out``.
+
+    Args:
+        out: Output frames (..., H, W), float32 or float64.  A CUDA tensor (or any
+            ``__cuda_array_interface__`` array) is updated in place on its device; a
+            host array (NumPy, CPU tensor) is staged through the GPU and updated in
+            place while the current device is 'cuda'.
+        lines: (N, 5) rows [x0, y0, x1, y1, width], xy order.
+        idxs: frame index of each line into the flattened leading dims of ``out``;
+            None draws every line into frame 0 (single frame) or line i into frame i.
+        max_val: peak value of a line's profile.
+        kernel: 'biweight', 'gaussian', 'parabolic', 'rectangular' or 'triangular'.
+        overlap: 'sum' or 'max' combination of overlapping lines.
+
+    Returns:
+        ``out``.
+    """
+    k, ov = _check_names(kernel, overlap)
+    if isinstance(out, torch.Tensor):
+        if out.is_cuda:
+            return _draw_lines_cuda(out, lines, idxs, max_val, k, ov)
+        host = out
+    elif hasattr(out, '__cuda_array_interface__'):
+        _draw_lines_cuda(torch.as_tensor(out, device='cuda'), lines, idxs, max_val, k, ov)
+        return out
+    else:
+        host = out
+    if _device.get_device() != 'cuda':
+        raise RuntimeError("cbclib_v2_gb300 has no CPU implementation of draw_lines: select "
+                           "the 'cuda' device or pass CUDA arrays")
+    if isinstance(host, torch.Tensor):
+        if host.dtype not in (torch.float32, torch.float64):
+            raise TypeError(f"out must be float32 or float64, got {host.dtype}")
+        dev_out = host.to('cuda')
+        _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov)
+        host.copy_(dev_out)
+        return out
+    if not isinstance(host, np.ndarray):
+        raise TypeError(f"unsupported output array type {type(out)}")
+    if host.dtype not in (np.float32, np.float64):
+        raise TypeError(f"out must be float32 or float64, got {host.dtype}")
+    dev_out = torch.from_numpy(np.ascontiguousarray(host)).to('cuda')
+    _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov)
+    if host.flags.c_contiguous and host.flags.writeable:
+        torch.from_numpy(host).copy_(dev_out)
+    else:
+        np.copyto(host, dev_out.cpu().numpy())
+    return out

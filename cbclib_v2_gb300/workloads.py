@@ -1,0 +1,82 @@
+"""Seeded synthetic line sets with the shapes and distributions of the benchmark
+workloads (no dataset ships with the reference; these stand in for detector frames).
+
+Every generator returns float64 NumPy arrays ``lines`` (N, 5) = [x0, y0, x1, y1, w]
+and ``idxs`` (N,) frame indices sorted by frame, plus the frame shape.
+"""
+from dataclasses import dataclass
+from typing import Tuple
+
+import numpy as np
+
+
+@dataclass
+class LineSet:
+    name: str
+    shape: Tuple[int, int, int]      # (frames, height, width)
+    lines: np.ndarray                # (N, 5) float64
+    idxs: np.ndarray                 # (N,) int64, non-decreasing
+    kernel: str
+    overlap: str
+    max_val: float = 1.0
+
+    @property
+    def n_lines(self) -> int:
+        return int(self.lines.shape[0])
+
+    def frame_offsets(self) -> np.ndarray:
+        """CSR offsets (F + 1,) of the lines of each frame."""
+        return np.searchsorted(self.idxs, np.arange(self.shape[0] + 1)).astype(np.int64)
+
+
+def _segments(rng, n, H, W, lengths, widths):
+    p0 = rng.random((n, 2)) * np.array([W, H], dtype=np.float64)
+    ang = rng.random(n) * 2.0 * np.pi
+    p1 = p0 + lengths[:, None] * np.stack([np.cos(ang), np.sin(ang)], axis=-1)
+    return np.concatenate([p0, p1, widths[:, None]], axis=-1)
+
+
+def single_frame(seed: int = 0, H: int = 512, W: int = 512, n: int = 1000) -> LineSet:
+    """One 512x512 frame, 1,000 segments: uniform endpoints, length U(10, 100),
+    width U(1, 5), rectangular profile, sum overlap."""
+    rng = np.random.default_rng(seed)
+    lines = _segments(rng, n, H, W, rng.uniform(10, 100, n), rng.uniform(1, 5, n))
+    return LineSet('single_frame_512', (1, H, W), lines, np.zeros(n, np.int64),
+                   'rectangular', 'sum')
+
+
+def detector_stack(seed: int = 0, F: int = 64, H: int = 2167, W: int = 2070,
+                   mean_lines: float = 2000.0) -> LineSet:
+    """64 detector frames of 2167x2070: Poisson(2,000) segments per frame, uniform
+    endpoints, lognormal length (median 40 px, sigma 0.6) clipped to [5, 400],
+    width U(1.5, 4), gaussian profile, max overlap."""
+    rng = np.random.default_rng(seed)
+    counts = rng.poisson(mean_lines, F)
+    n = int(counts.sum())
+    lengths = np.clip(rng.lognormal(np.log(40.0), 0.6, n), 5.0, 400.0)
+    lines = _segments(rng, n, H, W, lengths, rng.uniform(1.5, 4.0, n))
+    idxs = np.repeat(np.arange(F, dtype=np.int64), counts)
+    return LineSet(f'detector_stack_{F}x{H}x{W}', (F, H, W), lines, idxs, 'gaussian', 'max')
+
+
+def ragged_stack(seed: int = 0, F: int = 256, H: int = 1024, W: int = 1024,
+                 median: float = 1500.0, sigma: float = 1.0) -> LineSet:
+    """256 frames of 1024x1024 with lognormal segment counts (median 1,500, sigma 1.0)
+    clipped to [100, 20,000]; segments as in the single-frame workload; triangular
+    profile, sum overlap."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(rng.lognormal(np.log(median), sigma, F)), 100, 20000).astype(int)
+    n = int(counts.sum())
+    lines = _segments(rng, n, H, W, rng.uniform(10, 100, n), rng.uniform(1, 5, n))
+    idxs = np.repeat(np.arange(F, dtype=np.int64), counts)
+    return LineSet(f'ragged_stack_{F}x{H}x{W}', (F, H, W), lines, idxs, 'triangular', 'sum')
+
+
+def frames_subset(ls: LineSet, frames) -> LineSet:
+    """The lines of some frames, re-indexed 0..len(frames)-1 (for CPU checks)."""
+    frames = np.asarray(frames, dtype=np.int64)
+    sel = np.isin(ls.idxs, frames)
+    remap = {int(f): i for i, f in enumerate(frames)}
+    idxs = np.array([remap[int(f)] for f in ls.idxs[sel]], dtype=np.int64)
+    return LineSet(ls.name + '_subset', (len(frames), ls.shape[1], ls.shape[2]),
+                   ls.lines[sel], idxs, ls.kernel, ls.overlap, ls.max_val)

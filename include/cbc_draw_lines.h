@@ -1,0 +1,135 @@
+/*
+ * cbc_draw_lines.h — C ABI of the GB300 (sm_103a) streak-model rasteriser.
+ *
+ * Every entry point takes plain pointers and sizes; device pointers are CUDA device
+ * memory of the current device, `stream` is a cudaStream_t (NULL = legacy default
+ * stream).  Calls are stream-ordered and never synchronise the host, except
+ * cbc_read_status(), which waits for the stream.  No C++ exception crosses the ABI.
+ *
+ * Reference interfaces replaced (paths inside the cbclib_v2 project):
+ *   bresenham.draw_lines           cbclib_v2/_src/src/bresenham.cpp:313-331 (pybind11,
+ *                                   overloads <double,long> and <float,int>)
+ *   cuda_draw_lines.draw_lines     cbclib_v2/_src/src/cuda_draw_lines.cu:1098-1113
+ *   cuda_draw_lines.accumulate_lines  cbclib_v2/_src/src/cuda_draw_lines.cu:1076-1097
+ * as called by cbclib_v2/_src/functions.py:235-254 (_draw_lines_cpu/_gpu) and
+ * :151-173 (_accumulate_lines_cpu/_gpu).
+ */
+#ifndef CBC_DRAW_LINES_H
+#define CBC_DRAW_LINES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CBC_API __attribute__((visibility("default")))
+#else
+#define CBC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (host return values and device status flags) ------------------ */
+#define CBC_OK              0
+#define CBC_ERR_INVALID     1   /* bad argument: ValueError in the reference           */
+#define CBC_ERR_INDEX       2   /* frame index out of range: IndexError (bresenham.cpp:32-34) */
+#define CBC_ERR_CAPACITY    3   /* pair buffer too small; nothing was drawn, retry      */
+#define CBC_ERR_CUDA        4   /* CUDA runtime error: RuntimeError (cupy_array.hpp:18-24) */
+#define CBC_ERR_RANGE       5   /* a line's walk is longer than CBC_MAX_WALK pixels     */
+
+#define CBC_MAX_WALK (1 << 22)
+
+/* profile kernels, enum order of kernels::type (include.hpp:470-479) */
+#define CBC_BIWEIGHT    0
+#define CBC_GAUSSIAN    1
+#define CBC_PARABOLIC   2
+#define CBC_RECTANGULAR 3
+#define CBC_TRIANGULAR  4
+
+/* overlap modes (bresenham.cpp:142-149: "sum" -> 0, "max" -> 1) */
+#define CBC_SUM 0
+#define CBC_MAX 1
+
+/* tile shape of the render pass; zeros select the built-in default */
+typedef struct cbc_tuning {
+    int32_t tile_w;        /* tile width in pixels (x), multiple of 4, 16..256        */
+    int32_t tile_h;        /* tile height in pixels (y), 4..256                       */
+    int32_t chunk_lines;   /* lines staged per shared-memory chunk, 1..32             */
+    int32_t reserved;
+} cbc_tuning;
+
+/* device-side status, the first bytes of the workspace, read by cbc_read_status */
+typedef struct cbc_status {
+    int32_t flags;         /* bit (1 << CBC_ERR_x) for every error seen               */
+    int32_t reserved;
+    int64_t bad_line;      /* smallest offending line index (INT64_MAX if none)       */
+    int64_t idx_min;       /* smallest frame index in idxs (INT64_MAX if none)        */
+    int64_t idx_max;       /* largest frame index in idxs (INT64_MIN if none)         */
+    int64_t pairs_needed;  /* (line, tile) pairs the call produced                    */
+} cbc_status;
+
+/* Bytes of device workspace a call with these sizes needs.  `pair_capacity` bounds
+ * the (line, tile) pairs; when a call produces more, it draws nothing, sets
+ * CBC_ERR_CAPACITY and reports the count in pairs_needed, so the caller can grow the
+ * workspace and repeat the call. */
+CBC_API size_t cbc_draw_lines_workspace_size(int64_t n_frames, int64_t height, int64_t width,
+                                     int64_t n_lines, int64_t pair_capacity,
+                                     int32_t elem_bytes, const cbc_tuning *tuning);
+
+/* draw_lines: out[(f, y, x)] = out ⊕ max_val·K(d/w) for every pixel the reference's
+ * Bresenham walk of each line visits with error <= 1, ⊕ = + (CBC_SUM) or max (CBC_MAX).
+ *   out    (n_frames, height, width) C-contiguous, updated in place
+ *   lines  (n_lines, 5) C-contiguous rows x0, y0, x1, y1, width (xy order)
+ *   idxs   (n_lines,) frame of each line, int32 (idx_bytes = 4) or int64 (8);
+ *          NULL: frame 0 when n_frames == 1, frame i when n_frames == n_lines
+ *          (bresenham.cpp:5-20), otherwise CBC_ERR_INVALID.
+ * Returns CBC_OK or a host-detected error; device-detected errors (frame index out
+ * of range, capacity, walk range) are left in the workspace status and leave `out`
+ * untouched. */
+CBC_API int cbc_draw_lines_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
+                       const float *lines, int64_t n_lines, const void *idxs,
+                       int32_t idx_bytes, float max_val, int32_t kernel, int32_t overlap,
+                       void *workspace, size_t workspace_bytes, int64_t pair_capacity,
+                       const cbc_tuning *tuning, void *stream);
+
+CBC_API int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
+                       const double *lines, int64_t n_lines, const void *idxs,
+                       int32_t idx_bytes, double max_val, int32_t kernel, int32_t overlap,
+                       void *workspace, size_t workspace_bytes, int64_t pair_capacity,
+                       const cbc_tuning *tuning, void *stream);
+
+/* Wait for `stream` and copy the device status of the last call that used
+ * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
+CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
+
+/* Per-stage device time of the calls made while profiling is on, from CUDA events
+ * recorded on each call's stream around its kernels (no effect on results). */
+typedef struct cbc_profile {
+    int32_t calls;         /* calls measured since the last reset                    */
+    int32_t reserved;
+    double ms_prep;        /* status init + line records + tile counts               */
+    double ms_offsets;     /* bin offsets                                            */
+    double ms_fill;        /* (line, tile) pair fill                                 */
+    double ms_render;      /* tile render (the dominant kernel)                      */
+} cbc_profile;
+
+/* Turn the per-stage event timing on (1) or off (0); returns the previous state. */
+CBC_API int cbc_profile_enable(int32_t on);
+
+/* Wait for the recorded events, add their times into *profile (zeroed first when
+ * `reset` is 1, which also clears the accumulated calls).  Returns CBC_OK or
+ * CBC_ERR_CUDA. */
+CBC_API int cbc_profile_read(cbc_profile *profile, int32_t reset);
+
+/* Message of the last host-side error on the calling thread ("" if none). */
+CBC_API const char *cbc_last_error(void);
+
+/* Library version string. */
+CBC_API const char *cbc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CBC_DRAW_LINES_H */

@@ -47,3 +47,15 @@ float cbc_oracle_pixel_error_f32(float te, float ne, float len, float width)
     it.ne[0] = ne;
     return oerror_f32(&p, &it, width);
 }
+
+/* batch forms for the tests of the float emulation in the GPU kernels */
+void cbc_oracle_profile_batch_f32(int kernel, const float *x, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) out[i] = oprofile_f32(kernel, x[i]);
+}
+
+void cbc_oracle_pixel_error_batch_f32(const float *te, const float *ne, const float *len,
+                                      const float *width, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) out[i] = cbc_oracle_pixel_error_f32(te[i], ne[i], len[i], width[i]);
+}

@@ -1,0 +1,36 @@
+/* Host build of the GPU kernels' float emulation (cbclib_v2_gb300/csrc/exact.cuh) so the
+ * tests can compare it with the oracle on the CPU.  Built with -ffp-contract=off. */
+#include <stdint.h>
+static long long cbc_slow_count = 0;
+#include "exact.cuh"
+
+void exact_profile_batch(int kernel, const float *x, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) out[i] = cbc_profile_f32(kernel, x[i]);
+}
+
+void exact_pixel_error_batch(const float *te, const float *ne, const float *len,
+                             const float *width, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) {
+        float w = width[i];
+        if (!(w > 0.0f)) { out[i] = 1.0f / 0.0f; continue; }
+        float nf = cbc_normal_term(ne[i], len[i]);
+        out[i] = cbc_pixel_error(te[i], nf, len[i], len[i] * len[i], w * w);
+    }
+}
+
+/* fraction of evaluations that leave the float fast path */
+void exact_fast_path_stats(int which, const float *x, int64_t n, int64_t *slow)
+{
+    int64_t s = 0;
+    for (int64_t i = 0; i < n; i++) {
+        float r;
+        if (which == 0) {   /* one_minus_sq */
+            float v = x[i];
+            float p = v * v, pe = fmaf(v, v, -p), t = 1.0f - p, z = t - 1.0f, e = -p - z;
+            s += !cbc_ff_round(t, e - pe, &r);
+        }
+    }
+    *slow = s;
+}

@@ -1,0 +1,83 @@
+"""The GPU kernels' float emulation of the reference's double-rounded per-pixel steps
+(cbclib_v2_gb300/csrc/exact.cuh) is compiled here as host C and compared bit for bit
+with the oracle on random and adversarial inputs."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, 'cbclib_v2_gb300', 'csrc')
+
+
+@pytest.fixture(scope='module')
+def exact(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp('exact') / 'libexact_host.so')
+    subprocess.run(['gcc', '-O2', '-std=c11', '-ffp-contract=off', '-fPIC', '-shared',
+                    '-I', CSRC, os.path.join(ROOT, 'tests', 'native', 'exact_host.c'),
+                    '-o', out, '-lm'], check=True)
+    lib = ctypes.CDLL(out)
+    P = ctypes.c_void_p
+    lib.exact_profile_batch.argtypes = [ctypes.c_int, P, P, ctypes.c_int64]
+    lib.exact_pixel_error_batch.argtypes = [P] * 5 + [ctypes.c_int64]
+    return lib
+
+
+@pytest.fixture(scope='module')
+def olib():
+    lib = oracle._load()
+    P = ctypes.c_void_p
+    lib.cbc_oracle_profile_batch_f32.argtypes = [ctypes.c_int, P, P, ctypes.c_int64]
+    lib.cbc_oracle_pixel_error_batch_f32.argtypes = [P] * 5 + [ctypes.c_int64]
+    return lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _xs(rng, n):
+    near_one = np.arange(np.float32(0.9995).view(np.uint32), np.float32(1.0).view(np.uint32) + 1,
+                         dtype=np.uint32).view(np.float32)
+    return [rng.random(n, dtype=np.float32),
+            np.sqrt(rng.random(n, dtype=np.float32)),
+            (rng.random(n, dtype=np.float32) ** 8).astype(np.float32),
+            (1 - rng.random(n, dtype=np.float32) * 1e-3).astype(np.float32),
+            near_one, np.array([0.0, 1.0, 0.5, 1e-30, 1e-12], np.float32)]
+
+
+@pytest.mark.parametrize("kernel", list(oracle.KERNELS))
+def test_profiles_bit_exact(exact, olib, kernel):
+    rng = np.random.default_rng(11)
+    k = oracle.KERNELS[kernel]
+    for x in _xs(rng, 400_000):
+        x = np.ascontiguousarray(x)
+        a = np.empty_like(x)
+        b = np.empty_like(x)
+        olib.cbc_oracle_profile_batch_f32(k, _p(x), _p(a), x.size)
+        exact.exact_profile_batch(k, _p(x), _p(b), x.size)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ['body', 'caps', 'near_line'])
+def test_pixel_error_bit_exact(exact, olib, mode):
+    rng = np.random.default_rng({'body': 1, 'caps': 2, 'near_line': 3}[mode])
+    m = 600_000
+    ln = (rng.random(m) * 100 + 0.01).astype(np.float32)
+    w = (rng.random(m) * 6 + 0.05).astype(np.float32)
+    te = ((rng.random(m) * 1.4 - 0.2) * ln * ln).astype(np.float32)
+    ne = ((rng.random(m) * 2 - 1) * w * ln * 1.2).astype(np.float32)
+    if mode == 'caps':
+        te = (ln * ln + (rng.random(m) * 2 - 1) * w * ln).astype(np.float32)
+    if mode == 'near_line':
+        ne = (ne * 1e-3).astype(np.float32)
+        te = ((rng.random(m) * 2 - 1) * w * ln).astype(np.float32)
+    a = np.empty(m, np.float32)
+    b = np.empty(m, np.float32)
+    olib.cbc_oracle_pixel_error_batch_f32(_p(te), _p(ne), _p(ln), _p(w), _p(a), m)
+    exact.exact_pixel_error_batch(_p(te), _p(ne), _p(ln), _p(w), _p(b), m)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
