@@ -272,12 +272,21 @@ def main():
 
     peak, peak_src = measured_peak()
     render_ms = prof.ms_render / max(prof.calls, 1)
-    algo_bytes = 2 * F * H * W * 4 + N * 24
+    # bytes the op must move: every 32-byte sector of `out` holding a drawn pixel is
+    # read and written once (all other sectors are untouched), plus each line's
+    # 5 coordinates and frame index
+    drawn_sectors = int(out.reshape(-1, 8).ne(0).any(dim=1).sum().item())
+    algo_bytes = 64 * drawn_sectors + N * 24
+    full_bytes = 2 * F * H * W * 4 + N * 24
     achieved = algo_bytes / (render_ms * 1e-3) / 1e9
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_src,
                 'traffic': committed_traffic(ls.name), 'kernel': 'render_kernel',
-                'algorithmic_bytes': algo_bytes, 'ms_per_launch': render_ms,
+                'algorithmic_bytes': algo_bytes,
+                'bytes_model': 'read+write of each 32 B sector holding a drawn pixel '
+                               '(%d of %d sectors) + 24 B per line' % (drawn_sectors, F * H * W // 8),
+                'full_frame_rmw_frac': full_bytes / (render_ms * 1e-3) / 1e9 / peak,
+                'ms_per_launch': render_ms,
                 'stage_ms_per_call': {
                     'prep': prof.ms_prep / max(prof.calls, 1),
                     'offsets': prof.ms_offsets / max(prof.calls, 1),

@@ -12,6 +12,8 @@ from . import build as _build
 CBC_OK, CBC_ERR_INVALID, CBC_ERR_INDEX, CBC_ERR_CAPACITY, CBC_ERR_CUDA, CBC_ERR_RANGE = range(6)
 MAX_WALK = 1 << 22
 
+STRATEGY_AUTO, STRATEGY_TILES, STRATEGY_LINES = 0, 1, 2
+
 KERNELS = {'biweight': 0, 'gaussian': 1, 'parabolic': 2, 'rectangular': 3, 'triangular': 4}
 OVERLAPS = {'sum': 0, 'max': 1}
 
@@ -19,14 +21,16 @@ OVERLAPS = {'sum': 0, 'max': 1}
 class Tuning(ctypes.Structure):
     """cbc_tuning: render tile shape and lines per shared-memory chunk (0 = default)."""
     _fields_ = [('tile_w', ctypes.c_int32), ('tile_h', ctypes.c_int32),
-                ('chunk_lines', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+                ('chunk_lines', ctypes.c_int32), ('threads', ctypes.c_int32),
+                ('strategy', ctypes.c_int32), ('reserved', ctypes.c_int32)]
 
 
 class Status(ctypes.Structure):
     """cbc_status: device-side result flags of the last call on a workspace."""
     _fields_ = [('flags', ctypes.c_int32), ('reserved', ctypes.c_int32),
                 ('bad_line', ctypes.c_int64), ('idx_min', ctypes.c_int64),
-                ('idx_max', ctypes.c_int64), ('pairs_needed', ctypes.c_int64)]
+                ('idx_max', ctypes.c_int64), ('pairs_needed', ctypes.c_int64),
+                ('checkpoints_needed', ctypes.c_int64)]
 
     def has(self, code: int) -> bool:
         return bool(self.flags & (1 << code))
@@ -50,13 +54,13 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
 
 def _declare(lib):
     p, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
-    lib.cbc_draw_lines_workspace_size.argtypes = [i64, i64, i64, i64, i64, i32,
+    lib.cbc_draw_lines_workspace_size.argtypes = [i64, i64, i64, i64, i64, i64, i32,
                                                   ctypes.POINTER(Tuning)]
     lib.cbc_draw_lines_workspace_size.restype = ctypes.c_size_t
     for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
         f = getattr(lib, 'cbc_draw_lines_' + sfx)
         f.argtypes = [p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, ctypes.c_size_t,
-                      i64, ctypes.POINTER(Tuning), p]
+                      i64, i64, ctypes.POINTER(Tuning), p]
         f.restype = ctypes.c_int
     lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
     lib.cbc_read_status.restype = ctypes.c_int

@@ -49,7 +49,7 @@ constexpr int kInvalidEntry = INT_MIN;
 
 /* ---- per-line walk record ------------------------------------------------------ */
 
-enum : int { kAxisY = 1, kStepXNeg = 2, kStepYNeg = 4, kDrawable = 8 };
+enum : int { kAxisY = 1, kStepXNeg = 2, kStepYNeg = 4, kDrawable = 8, kFastDiv = 16 };
 
 /* BresenhamPlotter state of one 2-D line (bresenham.hpp:243-263): the walk starts at
  * (x0, y0) = m_pt0 and ends when a coordinate reaches (x1, y1) = m_pt1 (step added). */
@@ -61,7 +61,23 @@ struct alignas(16) LineRec {
     T w, ww;         /* width, width * width                                   */
     T te0, ne0;      /* tangent / normal errors at the walk start              */
     T px, py;        /* pt0, for the tile coverage only                        */
+    T rlen, rww;     /* RN(1 / len), RN(1 / ww) for the division shortcut      */
+    T ne_thr;        /* spans continue while |ne| < ne_thr (see span_threshold) */
     int32_t frame, flags;
+    int32_t c0;      /* first in-frame long coordinate of the walk, in walk order  */
+    int32_t ncols;   /* in-frame long coordinates of the walk                      */
+    int32_t ck_base; /* index of the line's first walk checkpoint                  */
+    int32_t pad;
+};
+
+/* the walk's exact iterator state at the first position whose walk index
+ * (c - c0) * step_long reaches a multiple of kSeg (cx = INT_MIN: the walk ends first) */
+constexpr int kSeg = 8;
+
+template <typename T>
+struct Checkpoint {
+    int32_t cx, cy;
+    T te, ne;
 };
 
 /* status block at the start of the workspace */
@@ -72,6 +88,33 @@ struct DevStatus {
     long long idx_min;
     long long idx_max;
     unsigned long long pairs;      /* running pair cursor == pairs_needed */
+    unsigned long long cks;        /* running checkpoint cursor            */
+};
+
+/* per line of the current render chunk */
+template <typename T>
+struct SlotParams {
+    T ts, ns;           /* tangent / normal derivative along the short axis           */
+    T len, len2, ww;
+    T rlen, rww;
+    T ne_thr;           /* span continuation threshold on |ne|                         */
+    int ss;             /* step sign along the short axis (first span half)            */
+    int axis;
+    int fast;           /* len and ww in the range of the division shortcut            */
+};
+
+/* per line of the current render chunk: what the segment replays need */
+template <typename T>
+struct WalkSlot {
+    T d0t, d1t, d0n, d1n;   /* step * tangent, step * normal per axis     */
+    int sx, sy;
+    int x1, y1;             /* walk end                                   */
+    int c0, sa;             /* walk index = (c - c0) * sa                 */
+    int k_lo, k_hi;         /* walk indices of the in-tile columns        */
+    int ck_base;
+    int ent_base;           /* entry pool index of walk index k_lo        */
+    int seg_base;           /* first flattened segment item of this line  */
+    int axis;
 };
 
 /* ---- arithmetic in the reference's rounding ----------------------------------- */
@@ -84,16 +127,20 @@ template <> struct Ar<float> {
     static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
     static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
     static __device__ __forceinline__ float from_int(int v) { return __int2float_rn(v); }
-    static __device__ __forceinline__ float normal_term(float ne, float len) {
-        return cbc_normal_term(ne, len);
+    static __device__ __forceinline__ float nterm(float ne, const SlotParams<float> &p) {
+        return p.fast ? cbc_normal_term_r(ne, p.len, p.rlen) : cbc_normal_term(ne, p.len);
     }
-    static __device__ __forceinline__ float error(float te, float nf, float len, float len2,
-                                                  float ww) {
-        return cbc_pixel_error(te, nf, len, len2, ww);
+    static __device__ __forceinline__ float error(float te, float nf, const SlotParams<float> &p) {
+        return p.fast ? cbc_pixel_error_r(te, nf, p.len, p.len2, p.ww, p.rlen, p.rww)
+                      : cbc_pixel_error(te, nf, p.len, p.len2, p.ww);
     }
     template <int K>
     static __device__ __forceinline__ float profile(float x) { return cbc_profile_f32(K, x); }
+    static __device__ __forceinline__ bool fast_range(float v) {
+        return v >= CBC_DIV_LO && v <= CBC_DIV_HI;
+    }
 };
 
 template <> struct Ar<double> {
@@ -102,29 +149,63 @@ template <> struct Ar<double> {
     static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
     static __device__ __forceinline__ double sqrt(double a) { return __dsqrt_rn(a); }
+    static __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
     static __device__ __forceinline__ double from_int(int v) { return (double)v; }
     /* normal_error: T accumulator fed with pow(b, 2) = fl(b * b) (bresenham.hpp:284-289) */
-    static __device__ __forceinline__ double normal_term(double ne, double len) {
-        double b = __ddiv_rn(ne, len);
+    static __device__ __forceinline__ double nterm(double ne, const SlotParams<double> &p) {
+        double b = __ddiv_rn(ne, p.len);
         return __dmul_rn(b, b);
     }
     /* error(): fl(fl(fl(a * a) + nf) / ww) (bresenham.hpp:291-296) */
-    static __device__ __forceinline__ double error(double te, double nf, double len,
-                                                   double len2, double ww) {
-        double m1 = -te, m2 = __dsub_rn(te, len2);
+    static __device__ __forceinline__ double error(double te, double nf,
+                                                   const SlotParams<double> &p) {
+        double m1 = -te, m2 = __dsub_rn(te, p.len2);
         double ta = (m1 < m2) ? m2 : m1;
         if (ta < 0.0) ta = 0.0;
-        double a = __ddiv_rn(ta, len);
-        return __ddiv_rn(__dadd_rn(__dmul_rn(a, a), nf), ww);
+        double a = __ddiv_rn(ta, p.len);
+        return __ddiv_rn(__dadd_rn(__dmul_rn(a, a), nf), p.ww);
     }
     template <int K>
     static __device__ __forceinline__ double profile(double x) { return cbc_profile_f64(K, x); }
+    static __device__ __forceinline__ bool fast_range(double) { return false; }
 };
 
 /* ---- line preparation ---------------------------------------------------------- */
 
 template <typename T>
 __device__ __forceinline__ bool finite_val(T v) { return isfinite(v); }
+
+/* The span loops of draw_line_2d continue while normal_error < width^2, with
+ * normal_error = fl(fl(ne / len)^2) (bresenham.hpp:369-380).  That is a monotone
+ * function of |ne| (round-to-nearest is monotone and odd), so the test equals
+ * |ne| < ne_thr for ne_thr = the least non-negative float with
+ * fl(fl(ne_thr / len)^2) >= ww, found by bisection over the float bit patterns. */
+template <typename T>
+__device__ T span_threshold(T len, T ww);
+
+template <>
+__device__ float span_threshold<float>(float len, float ww)
+{
+    unsigned lo = 0u, hi = 0x7f800000u;              /* f(+inf) = inf >= ww */
+    while (lo < hi) {
+        unsigned mid = lo + ((hi - lo) >> 1);
+        float b = __fdiv_rn(__uint_as_float(mid), len);
+        if (__fmul_rn(b, b) >= ww) hi = mid; else lo = mid + 1;
+    }
+    return __uint_as_float(lo);
+}
+
+template <>
+__device__ double span_threshold<double>(double len, double ww)
+{
+    unsigned long long lo = 0ull, hi = 0x7ff0000000000000ull;
+    while (lo < hi) {
+        unsigned long long mid = lo + ((hi - lo) >> 1);
+        double b = __ddiv_rn(__longlong_as_double((long long)mid), len);
+        if (__dmul_rn(b, b) >= ww) hi = mid; else lo = mid + 1;
+    }
+    return __longlong_as_double((long long)lo);
+}
 
 /* BresenhamPlotter(line, long(ceil(width) + 1)) (bresenham.hpp:243-253) plus begin()
  * (:255-263).  Returns false for lines that draw nothing in the reference (zero
@@ -181,7 +262,12 @@ __device__ bool build_rec(const T *ln, LineRec<T> &r, bool &too_long)
     r.ne0 = A::add(A::mul(t1, d0), A::mul(-t0, d1));
     r.px = p0x;
     r.py = p0y;
-    r.flags = axis | (sx < 0 ? kStepXNeg : 0) | (sy < 0 ? kStepYNeg : 0) | kDrawable;
+    r.rlen = A::rcp(len);
+    r.rww = A::rcp(r.ww);
+    bool fast = A::fast_range(len) && A::fast_range(r.ww);
+    r.ne_thr = span_threshold<T>(len, r.ww);
+    r.flags = axis | (sx < 0 ? kStepXNeg : 0) | (sy < 0 ? kStepYNeg : 0) | kDrawable |
+              (fast ? kFastDiv : 0);
     return true;
 }
 
@@ -191,38 +277,84 @@ struct Geometry {
     int tiles_x, tiles_y;
 };
 
-/* Conservative set of tiles holding the pixels the walk can draw: the walk covers the
+/* Conservative tile coverage of the pixels the walk can draw.  The walk covers the
  * long-axis range [m_pt0, m_pt1) exactly; at long coordinate c its centre pixel lies
  * within 1 px of the line and its spans stop where |normal distance| >= width, i.e.
  * within width * len / |t_long| of the line along the short axis. */
-template <typename T, typename Fn>
-__device__ void for_each_tile(const LineRec<T> &r, const Geometry &g, Fn fn)
-{
-    const int a = r.flags & kAxisY;
-    const int sxs = (r.flags & kStepXNeg) ? -1 : 1, sys = (r.flags & kStepYNeg) ? -1 : 1;
-    const int sa = a ? sys : sxs;
-    int first = a ? r.y0 : r.x0;
-    int last = (a ? r.y1 : r.x1) - sa;
-    int lmin = min(first, last), lmax = max(first, last);
-    const int ext_a = a ? g.H : g.W, ext_s = a ? g.W : g.H;
-    const int TA = a ? g.tile_h : g.tile_w, TS = a ? g.tile_w : g.tile_h;
-    lmin = max(lmin, 0);
-    lmax = min(lmax, ext_a - 1);
-    if (lmin > lmax) return;
-    const float ta = (float)(a ? r.t1 : r.t0), ts = (float)(a ? r.t0 : r.t1);
-    const float pa = (float)(a ? r.py : r.px), ps = (float)(a ? r.px : r.py);
-    const float slope = ts / ta;
-    const float hw = (float)r.w * (float)r.len / fabsf(ta) + 2.0f;
-    for (int ti = lmin / TA; ti <= lmax / TA; ti++) {
+template <typename T>
+struct Coverage {
+    int a, sa;          /* long axis, walk direction along it                          */
+    int lmin, lmax;     /* long-axis range of the walk inside the frame                */
+    int TA, TS;         /* tile extents along the long / short axis                    */
+    int ext_s;
+    float ps, pa, slope, hw;
+
+    __device__ bool init(const LineRec<T> &r, const Geometry &g) {
+        a = r.flags & kAxisY;
+        const int sxs = (r.flags & kStepXNeg) ? -1 : 1, sys = (r.flags & kStepYNeg) ? -1 : 1;
+        sa = a ? sys : sxs;
+        int first = a ? r.y0 : r.x0;
+        int last = (a ? r.y1 : r.x1) - sa;
+        lmin = max(min(first, last), 0);
+        const int ext_a = a ? g.H : g.W;
+        ext_s = a ? g.W : g.H;
+        lmax = min(max(first, last), ext_a - 1);
+        TA = a ? g.tile_h : g.tile_w;
+        TS = a ? g.tile_w : g.tile_h;
+        const float ta = (float)(a ? r.t1 : r.t0), ts = (float)(a ? r.t0 : r.t1);
+        pa = (float)(a ? r.py : r.px);
+        ps = (float)(a ? r.px : r.py);
+        slope = ts / ta;
+        hw = (float)r.w * (float)r.len / fabsf(ta) + 2.0f;
+        return lmin <= lmax;
+    }
+    /* tile rows (short-axis tile indices) [j0, j1] of tile column ti; false if none */
+    __device__ bool rows(int ti, int &j0, int &j1) const {
         int ca = max(lmin, ti * TA), cb = min(lmax, ti * TA + TA - 1);
         float s0 = ps + ((float)ca - pa) * slope, s1 = ps + ((float)cb - pa) * slope;
         float smin = fminf(s0, s1) - hw, smax = fmaxf(s0, s1) + hw;
-        if (!(smax >= 0.0f) || !(smin <= (float)(ext_s - 1))) continue;
-        int j0 = max(0, (int)floorf(fmaxf(smin, -1.0f))) / TS;
-        int j1 = min(ext_s - 1, (int)floorf(fminf(smax, (float)ext_s))) / TS;
-        for (int tj = j0; tj <= j1; tj++) fn(a ? (ti * g.tiles_x + tj) : (tj * g.tiles_x + ti));
+        if (!(smax >= 0.0f) || !(smin <= (float)(ext_s - 1))) return false;
+        j0 = max(0, (int)floorf(fmaxf(smin, -1.0f))) / TS;
+        j1 = min(ext_s - 1, (int)floorf(fminf(smax, (float)ext_s))) / TS;
+        return j0 <= j1;
     }
-}
+    __device__ int bin(int ti, int tj, const Geometry &g) const {
+        return a ? (ti * g.tiles_x + tj) : (tj * g.tiles_x + ti);
+    }
+};
+
+/* the reference's outer-walk step (LineIterator::update + operator++, bresenham.hpp:
+ * 205-220 and 98-111, for the single axis pair of 2-D) */
+template <typename T>
+struct Walker {
+    int cx, cy;
+    T te, ne;
+    int sx, sy;
+    T d0t, d1t, d0n, d1n;   /* step * tangent, step * normal per axis */
+
+    __device__ void init(const LineRec<T> &r) {
+        sx = (r.flags & kStepXNeg) ? -1 : 1;
+        sy = (r.flags & kStepYNeg) ? -1 : 1;
+        d0t = sx > 0 ? r.t0 : -r.t0;
+        d1t = sy > 0 ? r.t1 : -r.t1;
+        d0n = sx > 0 ? r.t1 : -r.t1;
+        d1n = sy > 0 ? -r.t0 : r.t0;
+    }
+    /* decisions at the current position: (next x, next y) */
+    __device__ __forceinline__ void decide(bool &nx, bool &ny, T &exx) const {
+        using A = Ar<T>;
+        exx = A::add(ne, d0n);
+        T eyy = A::add(ne, d1n);
+        T exy = A::add(exx, d1n);
+        if (fabs(eyy) < fabs(exx)) { ny = true; nx = fabs(exy) < fabs(eyy); }
+        else                       { nx = true; ny = fabs(exy) < fabs(exx); }
+    }
+    __device__ __forceinline__ void step(bool nx, bool ny, T exx) {
+        using A = Ar<T>;
+        if (nx) { cx += sx; te = A::add(te, d0t); ne = exx; }
+        if (ny) { cy += sy; te = A::add(te, d1t); ne = A::add(ne, d1n); }
+    }
+};
 
 template <typename IdxT>
 __device__ __forceinline__ long long load_idx(const void *idxs, long long i)
@@ -248,33 +380,66 @@ template <typename T, typename IdxT>
 __global__ void __launch_bounds__(kThreads)
 prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
             long long n_frames, Geometry g, LineRec<T> *__restrict__ recs,
-            int *__restrict__ counts, DevStatus *st)
+            int *__restrict__ counts, long long ck_capacity, DevStatus *st)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool in = i < n_lines;
+    const bool in = i < n_lines;
     long long frame = 0;
-    bool has_idx = idxs != nullptr;
+    const bool has_idx = idxs != nullptr;
     if (in) frame = has_idx ? load_idx<IdxT>(idxs, i) : (n_frames == 1 ? 0 : i);
     if (has_idx) warp_minmax(frame, in, st);
-    if (!in) return;
     LineRec<T> r;
     r.flags = 0;
-    if (frame < 0 || frame >= n_frames) {
-        atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
-        atomicMin(&st->bad_line, (unsigned long long)i);
-        recs[i] = r;
-        return;
-    }
-    bool too_long = false;
-    if (build_rec(lines + 5 * i, r, too_long)) {
-        r.frame = (int32_t)frame;
-        int *fc = counts + (size_t)frame * g.tiles_x * g.tiles_y;
-        for_each_tile(r, g, [&](int b) { atomicAdd(fc + b, 1); });
-    } else {
-        r.flags = 0;
-        if (too_long) {
-            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+    int nck = 0;
+    Coverage<T> cv;
+    if (in) {
+        if (frame < 0 || frame >= n_frames) {
+            atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
             atomicMin(&st->bad_line, (unsigned long long)i);
+        } else {
+            bool too_long = false;
+            if (build_rec(lines + 5 * i, r, too_long)) {
+                r.frame = (int32_t)frame;
+                if (cv.init(r, g)) {
+                    r.ncols = cv.lmax - cv.lmin + 1;
+                    r.c0 = cv.sa > 0 ? cv.lmin : cv.lmax;
+                    nck = (r.ncols + kSeg - 1) / kSeg;
+                } else {
+                    r.flags = 0;        /* walk never enters the frame */
+                }
+            } else {
+                r.flags = 0;
+                if (too_long) {
+                    atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+                    atomicMin(&st->bad_line, (unsigned long long)i);
+                }
+            }
+        }
+    }
+    /* checkpoint blocks: one atomic per warp on the checkpoint cursor */
+    const int lane = threadIdx.x & 31;
+    int incl = nck;
+    for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    unsigned long long wbase = 0;
+    if (lane == 31) wbase = atomicAdd(&st->cks, (unsigned long long)incl);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    if (!in) return;
+    if (r.flags & kDrawable) {
+        unsigned long long cb = wbase + (unsigned long long)(incl - nck);
+        if (cb + (unsigned long long)nck > (unsigned long long)ck_capacity) {
+            atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+            r.ck_base = 0;
+        } else {
+            r.ck_base = (int32_t)cb;
+        }
+        int *fc = counts + (size_t)frame * g.tiles_x * g.tiles_y;
+        for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
+            int j0, j1;
+            if (!cv.rows(ti, j0, j1)) continue;
+            for (int tj = j0; tj <= j1; tj++) atomicAdd(fc + cv.bin(ti, tj, g), 1);
         }
     }
     recs[i] = r;
@@ -288,6 +453,7 @@ __global__ void init_status_kernel(DevStatus *st)
     st->idx_min = LLONG_MAX;
     st->idx_max = LLONG_MIN;
     st->pairs = 0;
+    st->cks = 0;
 }
 
 /* bin offsets: block-local exclusive scan + one atomic per block on the pair cursor */
@@ -327,22 +493,67 @@ offsets_kernel(const int *__restrict__ counts, int *__restrict__ offsets,
     fillpos[b] = o32;
 }
 
+/* one thread per line: write the line id into each of its bins, then walk the line
+ * once and store the iterator state every kSeg walk columns inside the frame */
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 fill_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
             int *__restrict__ fillpos, int *__restrict__ pairs, long long capacity,
-            const DevStatus *st)
+            Checkpoint<T> *__restrict__ cks, DevStatus *st)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_lines) return;
     if (st->flags & kFatal) return;
-    LineRec<T> r = recs[i];
+    const LineRec<T> r = recs[i];
     if (!(r.flags & kDrawable)) return;
+    Coverage<T> cv;
+    if (!cv.init(r, g)) return;
     int *fp = fillpos + (size_t)r.frame * g.tiles_x * g.tiles_y;
-    for_each_tile(r, g, [&](int b) {
-        int pos = atomicAdd(fp + b, 1);
-        if (pos < capacity) pairs[pos] = (int)i;
-    });
+    for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
+        int j0, j1;
+        if (!cv.rows(ti, j0, j1)) continue;
+        for (int tj = j0; tj <= j1; tj++) {
+            int pos = atomicAdd(fp + cv.bin(ti, tj, g), 1);
+            if (pos < capacity) pairs[pos] = (int)i;
+        }
+    }
+    Walker<T> wk;
+    wk.init(r);
+    wk.cx = r.x0;
+    wk.cy = r.y0;
+    wk.te = r.te0;
+    wk.ne = r.ne0;
+    const int nck = (r.ncols + kSeg - 1) / kSeg;
+    Checkpoint<T> *ck = cks + r.ck_base;
+    int k = 0;
+    long long guard = 0;
+    while (k < nck && wk.cx != r.x1 && wk.cy != r.y1) {
+        const int idx = ((cv.a ? wk.cy : wk.cx) - r.c0) * cv.sa;
+        while (k < nck && idx >= k * kSeg) {
+            Checkpoint<T> c;
+            c.cx = wk.cx;
+            c.cy = wk.cy;
+            c.te = wk.te;
+            c.ne = wk.ne;
+            ck[k++] = c;
+        }
+        bool nx, ny;
+        T exx;
+        wk.decide(nx, ny, exx);
+        wk.step(nx, ny, exx);
+        if (++guard > 4LL * CBC_MAX_WALK + 64) {
+            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+            break;
+        }
+    }
+    for (; k < nck; k++) {
+        Checkpoint<T> c;
+        c.cx = INT_MIN;
+        c.cy = 0;
+        c.te = T(0);
+        c.ne = T(0);
+        ck[k] = c;
+    }
 }
 
 /* ---- render ---------------------------------------------------------------------- */
@@ -354,12 +565,18 @@ struct Entry {          /* one filled walk position (column) of a line inside th
     T te, ne;           /* tangent / normal errors there                              */
 };
 
-template <typename T>
-struct SlotParams {     /* per line of the current chunk */
-    T ts, ns;           /* tangent / normal derivative along the short axis           */
-    T len, len2, ww;
-    int ss;             /* step sign along the short axis (first span half)            */
-    int axis;
+template <typename T> struct Sentinel;
+/* sum: -0 is the only value that no contribution leaves behind (-0 + v = v, and
+ * -0 + +0 = +0); max: -inf, below every contribution that can change out */
+template <> struct Sentinel<float> {
+    static __device__ __forceinline__ float sum() { return -0.0f; }
+    static __device__ __forceinline__ bool sum_touched(float v) { return __float_as_uint(v) != 0x80000000u; }
+};
+template <> struct Sentinel<double> {
+    static __device__ __forceinline__ double sum() { return -0.0; }
+    static __device__ __forceinline__ bool sum_touched(double v) {
+        return (unsigned long long)__double_as_longlong(v) != 0x8000000000000000ull;
+    }
 };
 
 template <typename T>
@@ -368,7 +585,7 @@ __device__ __forceinline__ void combine_max(T *addr, T v);
 template <>
 __device__ __forceinline__ void combine_max<float>(float *addr, float v)
 {
-    /* out = std::max(out, v): replace only when out < v (bresenham.cpp:71) */
+    /* acc = std::max(acc, v): replace only when acc < v (bresenham.cpp:71) */
     unsigned *ua = reinterpret_cast<unsigned *>(addr);
     unsigned old = *reinterpret_cast<volatile unsigned *>(ua);
     while (__uint_as_float(old) < v) {
@@ -397,6 +614,7 @@ struct RenderArgs {
     const int *counts;
     const int *offsets;
     const int *pairs;
+    const Checkpoint<T> *cks;
     DevStatus *st;
     Geometry g;
     T max_val;
@@ -408,8 +626,8 @@ template <typename T>
 __host__ __device__ constexpr size_t render_smem_bytes(int tile_w, int tile_h, int ent_cap)
 {
     return (size_t)tile_w * tile_h * sizeof(T) + (size_t)ent_cap * sizeof(Entry<T>) +
-           (size_t)ent_cap + kMaxChunk * sizeof(SlotParams<T>) + (kMaxChunk + 1) * sizeof(int) +
-           64;
+           (size_t)ent_cap + kMaxChunk * sizeof(SlotParams<T>) +
+           kMaxChunk * sizeof(WalkSlot<T>) + 4 * sizeof(int) + 64;
 }
 
 template <typename T, int K, int OV>
@@ -430,100 +648,130 @@ render_kernel(RenderArgs<T> a)
     const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
     const int x0 = tx * g.tile_w, y0 = ty * g.tile_h;
     const int tw = min(g.tile_w, g.W - x0), th = min(g.tile_h, g.H - y0);
+    const int npix = tw * th;
 
-    T *tile = reinterpret_cast<T *>(smem);
-    Entry<T> *ent = reinterpret_cast<Entry<T> *>(tile + (size_t)g.tile_w * g.tile_h);
+    T *acc = reinterpret_cast<T *>(smem);
+    Entry<T> *ent = reinterpret_cast<Entry<T> *>(acc + (size_t)g.tile_w * g.tile_h);
     SlotParams<T> *prm = reinterpret_cast<SlotParams<T> *>(ent + a.ent_cap);
-    int *base = reinterpret_cast<int *>(prm + kMaxChunk);
-    unsigned char *eslot = reinterpret_cast<unsigned char *>(base + kMaxChunk + 1);
+    WalkSlot<T> *wsl = reinterpret_cast<WalkSlot<T> *>(prm + kMaxChunk);
+    int *totals = reinterpret_cast<int *>(wsl + kMaxChunk);          /* entries, segments */
+    unsigned char *eslot = reinterpret_cast<unsigned char *>(totals + 4);
 
-    T *gout = a.out + ((size_t)frame * g.H + y0) * g.W + x0;
-    for (int e = threadIdx.x; e < tw * th; e += kThreads) {
-        int r = e / tw, c = e - r * tw;
-        tile[e] = gout[(size_t)r * g.W + c];
-    }
+    const T init = OV == CBC_SUM ? Sentinel<T>::sum() : T(-INFINITY);
+    for (int e = threadIdx.x; e < npix; e += blockDim.x) acc[e] = init;
 
     const int *seg = a.pairs + a.offsets[bin];
     for (int cb = 0; cb < cnt; cb += a.chunk) {
         const int n = min(a.chunk, cnt - cb);
-        /* phase A: per-line slot parameters and the count of in-tile walk columns */
-        int my_count = 0, c_begin = 0, c_lo = 0, c_hi = -1, sa = 1;
-        LineRec<T> r;
-        if (threadIdx.x < n) {
-            r = a.recs[seg[cb + threadIdx.x]];
-            const int ax = r.flags & kAxisY;
-            const int sx = (r.flags & kStepXNeg) ? -1 : 1, sy = (r.flags & kStepYNeg) ? -1 : 1;
-            sa = ax ? sy : sx;
-            const int la0 = ax ? y0 : x0, la1 = ax ? y0 + th - 1 : x0 + tw - 1;
-            const int first = ax ? r.y0 : r.x0, last = (ax ? r.y1 : r.x1) - sa;
-            if (sa > 0) { c_lo = max(first, la0); c_hi = min(last, la1); c_begin = c_lo; }
-            else        { c_lo = max(last, la0);  c_hi = min(first, la1); c_begin = c_hi; }
-            my_count = max(0, c_hi - c_lo + 1);
-            SlotParams<T> p;
-            p.ts = ax ? r.t0 : r.t1;              /* d te / d short */
-            p.ns = ax ? r.t1 : -r.t0;             /* d ne / d short: normal = (t1, -t0) */
-            p.len = r.len;
-            p.len2 = r.len2;
-            p.ww = r.ww;
-            p.ss = ax ? sx : sy;
-            p.axis = ax;
-            prm[threadIdx.x] = p;
-        }
-        /* exclusive scan of the counts over the chunk (n <= 32: warp 0) */
+        /* phase A: per-line parameters, in-tile walk-index range, segment count */
         if (threadIdx.x < 32) {
-            int v = threadIdx.x < n ? my_count : 0, s = v;
-            for (int o = 1; o < 32; o <<= 1) {
-                int u = __shfl_up_sync(0xffffffffu, s, o);
-                if ((int)threadIdx.x >= o) s += u;
+            int my_count = 0, my_nseg = 0;
+            if ((int)threadIdx.x < n) {
+                const LineRec<T> r = a.recs[seg[cb + threadIdx.x]];
+                const int ax = r.flags & kAxisY;
+                const int sx = (r.flags & kStepXNeg) ? -1 : 1, sy = (r.flags & kStepYNeg) ? -1 : 1;
+                const int sa = ax ? sy : sx;
+                const int la0 = ax ? y0 : x0, la1 = ax ? y0 + th - 1 : x0 + tw - 1;
+                int k_lo = sa > 0 ? la0 - r.c0 : r.c0 - la1;
+                int k_hi = sa > 0 ? la1 - r.c0 : r.c0 - la0;
+                k_lo = max(k_lo, 0);
+                k_hi = min(k_hi, r.ncols - 1);
+                my_count = max(0, k_hi - k_lo + 1);
+                my_nseg = my_count > 0 ? k_hi / kSeg - k_lo / kSeg + 1 : 0;
+                SlotParams<T> p;
+                p.ts = ax ? r.t0 : r.t1;              /* d te / d short */
+                p.ns = ax ? r.t1 : -r.t0;             /* d ne / d short: normal = (t1, -t0) */
+                p.len = r.len;
+                p.len2 = r.len2;
+                p.ww = r.ww;
+                p.rlen = r.rlen;
+                p.rww = r.rww;
+                p.ne_thr = r.ne_thr;
+                p.ss = ax ? sx : sy;
+                p.axis = ax;
+                p.fast = (r.flags & kFastDiv) ? 1 : 0;
+                prm[threadIdx.x] = p;
+                WalkSlot<T> w;
+                w.sx = sx;
+                w.sy = sy;
+                w.d0t = sx > 0 ? r.t0 : -r.t0;
+                w.d1t = sy > 0 ? r.t1 : -r.t1;
+                w.d0n = sx > 0 ? r.t1 : -r.t1;
+                w.d1n = sy > 0 ? -r.t0 : r.t0;
+                w.x1 = r.x1;
+                w.y1 = r.y1;
+                w.c0 = r.c0;
+                w.sa = sa;
+                w.k_lo = k_lo;
+                w.k_hi = k_hi;
+                w.ck_base = r.ck_base;
+                w.axis = ax;
+                wsl[threadIdx.x] = w;
             }
-            base[threadIdx.x] = s - v;
-            if (threadIdx.x == 31) base[kMaxChunk] = s;
+            int ic = my_count, is = my_nseg;
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, ic, o);
+                int v = __shfl_up_sync(0xffffffffu, is, o);
+                if ((int)threadIdx.x >= o) { ic += u; is += v; }
+            }
+            if ((int)threadIdx.x < n) {
+                wsl[threadIdx.x].ent_base = ic - my_count;
+                wsl[threadIdx.x].seg_base = is - my_nseg;
+            }
+            if (threadIdx.x == 31) { totals[0] = ic; totals[1] = is; }
         }
         __syncthreads();
-        const int total = base[kMaxChunk];
-        for (int e = threadIdx.x; e < total; e += kThreads) ent[e].c = kInvalidEntry;
+        const int total = totals[0], nsegs = totals[1];
+        for (int e = threadIdx.x; e < total; e += blockDim.x) ent[e].c = kInvalidEntry;
         __syncthreads();
 
-        /* phase B: replay the walk (bresenham.hpp:352-383 outer loop) up to the tile */
-        if (threadIdx.x < n && my_count > 0) {
-            const int s = threadIdx.x;
-            const int my_base = base[s];
-            const int ax = r.flags & kAxisY;
-            const int sx = (r.flags & kStepXNeg) ? -1 : 1, sy = (r.flags & kStepYNeg) ? -1 : 1;
-            const T t0 = r.t0, t1 = r.t1;
-            const T d0t = sx > 0 ? t0 : -t0, d1t = sy > 0 ? t1 : -t1;   /* step * tau      */
-            const T d0n = sx > 0 ? t1 : -t1, d1n = sy > 0 ? -t0 : t0;   /* step * normal   */
-            const int far = sa > 0 ? c_hi : c_lo;
-            int cx = r.x0, cy = r.y0;
-            const int ex = r.x1, ey = r.y1;
-            T te = r.te0, ne = r.ne0;
-            long long guard = 0;
-            while (cx != ex && cy != ey) {
-                T exx = A::add(ne, d0n);
-                T eyy = A::add(ne, d1n);
-                T exy = A::add(exx, d1n);
+        /* phase B: every (line, kSeg-column segment) resumes the walk (bresenham.hpp:
+         * 352-383 outer loop) from its checkpoint, one thread each, and records the
+         * filled columns inside the tile */
+        for (int it = threadIdx.x; it < nsegs; it += blockDim.x) {
+            int sl = 0;
+            #pragma unroll
+            for (int bit = 16; bit > 0; bit >>= 1)
+                if (sl + bit < n && wsl[sl + bit].seg_base <= it) sl += bit;
+            const WalkSlot<T> &w = wsl[sl];
+            const int sg = w.k_lo / kSeg + (it - w.seg_base);
+            const Checkpoint<T> ck = a.cks[w.ck_base + sg];
+            if (ck.cx == INT_MIN) continue;
+            const int lo = max(sg * kSeg, w.k_lo), hi = min(sg * kSeg + kSeg - 1, w.k_hi);
+            Walker<T> wk;
+            wk.sx = w.sx;
+            wk.sy = w.sy;
+            wk.d0t = w.d0t;
+            wk.d1t = w.d1t;
+            wk.d0n = w.d0n;
+            wk.d1n = w.d1n;
+            wk.cx = ck.cx;
+            wk.cy = ck.cy;
+            wk.te = ck.te;
+            wk.ne = ck.ne;
+            int guard = 0;
+            while (wk.cx != w.x1 && wk.cy != w.y1) {
                 bool nx, ny;
-                if (fabs(eyy) < fabs(exx)) { ny = true; nx = fabs(exy) < fabs(eyy); }
-                else                       { nx = true; ny = fabs(exy) < fabs(exx); }
-                if (ax ? ny : nx) {
-                    const int c = ax ? cy : cx;
-                    if (c >= c_lo && c <= c_hi) {
-                        const int k = my_base + (c - c_begin) * sa;
+                T exx;
+                wk.decide(nx, ny, exx);
+                const int c = w.axis ? wk.cy : wk.cx;
+                const int idx = (c - w.c0) * w.sa;
+                if (w.axis ? ny : nx) {
+                    if (idx >= lo && idx <= hi) {
+                        const int k = w.ent_base + (idx - w.k_lo);
                         Entry<T> en;
                         en.c = c;
-                        en.sc = ax ? cx : cy;
-                        en.te = te;
-                        en.ne = ne;
+                        en.sc = w.axis ? wk.cx : wk.cy;
+                        en.te = wk.te;
+                        en.ne = wk.ne;
                         ent[k] = en;
-                        eslot[k] = (unsigned char)s;
-                        if (c == far) break;
-                    } else if ((c - far) * sa > 0) {
-                        break;
+                        eslot[k] = (unsigned char)sl;
+                        if (idx == hi) break;
                     }
                 }
-                if (nx) { cx += sx; te = A::add(te, d0t); ne = exx; }
-                if (ny) { cy += sy; te = A::add(te, d1t); ne = A::add(ne, d1n); }
-                if (++guard > 4LL * CBC_MAX_WALK + 64) {
+                if (idx > hi) break;
+                wk.step(nx, ny, exx);
+                if (++guard > 4 * CBC_MAX_WALK + 64) {
                     atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
                     break;
                 }
@@ -531,57 +779,330 @@ render_kernel(RenderArgs<T> a)
         }
         __syncthreads();
 
-        /* phase C: the centre and both span halves of every entry (bresenham.hpp:364-381) */
-        for (int e = threadIdx.x; e < total; e += kThreads) {
-            const Entry<T> en = ent[e];
-            if (en.c == kInvalidEntry) continue;
-            const SlotParams<T> p = prm[eslot[e]];
-            const int ax = p.axis;
-            const int s_lo = ax ? x0 : y0, s_hi = ax ? x0 + tw - 1 : y0 + th - 1;
-            T *trow = ax ? tile + ((ptrdiff_t)(en.c - y0) * tw - x0)
-                         : tile + ((ptrdiff_t)(en.c - x0) - (ptrdiff_t)y0 * tw);
-            const int sstride = ax ? 1 : tw;
-            /* centre pixel: always visited */
-            if (en.sc >= s_lo && en.sc <= s_hi) {
-                T nf = A::normal_term(en.ne, p.len);
-                T E = A::error(en.te, nf, p.len, p.len2, p.ww);
-                if (E <= T(1)) {
-                    T v = A::mul(a.max_val, A::template profile<K>(A::sqrt(E)));
-                    T *dst = trow + (ptrdiff_t)en.sc * sstride;
-                    if (OV == CBC_SUM) atomicAdd(dst, v); else combine_max(dst, v);
-                }
-            }
-            #pragma unroll 1
-            for (int half = 0; half < 2; half++) {
-                const int h = half ? -p.ss : p.ss;
-                if ((h > 0 && en.sc >= s_hi) || (h < 0 && en.sc <= s_lo)) continue;
-                const T dt = h > 0 ? p.ts : -p.ts, dn = h > 0 ? p.ns : -p.ns;
-                T te = en.te, ne = en.ne;
-                int y = en.sc;
-                for (int guard = 0; guard < 2 * CBC_MAX_WALK + 64; guard++) {
-                    y += h;
-                    te = A::add(te, dt);
-                    ne = A::add(ne, dn);
-                    T nf = A::normal_term(ne, p.len);
-                    if (!(nf < p.ww)) break;
-                    if (y >= s_lo && y <= s_hi) {
-                        T E = A::error(te, nf, p.len, p.len2, p.ww);
-                        if (E <= T(1)) {
-                            T v = A::mul(a.max_val, A::template profile<K>(A::sqrt(E)));
-                            T *dst = trow + (ptrdiff_t)y * sstride;
-                            if (OV == CBC_SUM) atomicAdd(dst, v); else combine_max(dst, v);
-                        }
+        /* phase C: the centre and both span halves of every entry (bresenham.hpp:364-381).
+         * Each warp flattens 32 entries into (entry, short offset j) items, one pixel
+         * per lane.  Pixel j != 0 lies |j| span steps from the centre: its errors are
+         * |j| sequential additions, and it is visited iff the first and the |j|-th
+         * step both pass the span test (the passing steps form an interval, because
+         * ne is monotone along a span and the test is a threshold on |ne|). */
+        {
+            const int lane = threadIdx.x & 31;
+            const int nwarps = blockDim.x >> 5;
+            for (int e0 = (threadIdx.x >> 5) * 32; e0 < total; e0 += nwarps * 32) {
+                const int e = e0 + lane;
+                int cnt = 0, jlo = 0;
+                if (e < total) {
+                    const Entry<T> en = ent[e];
+                    if (en.c != kInvalidEntry) {
+                        const SlotParams<T> &p = prm[eslot[e]];
+                        const int s_lo = p.axis ? x0 : y0, s_hi = p.axis ? x0 + tw - 1 : y0 + th - 1;
+                        /* conservative reach of the span: |ne| grows by |ns| per step */
+                        const float reach = ((float)p.ne_thr + fabsf((float)en.ne)) / fabsf((float)p.ns);
+                        const int J = reach < 2e9f ? (int)reach + 2 : INT_MAX / 4;
+                        jlo = max(-J, s_lo - en.sc);
+                        const int jhi = min(J, s_hi - en.sc);
+                        cnt = max(0, jhi - jlo + 1);
                     }
-                    if ((h > 0 && y >= s_hi) || (h < 0 && y <= s_lo)) break;
+                }
+                int incl = cnt;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                const int excl = incl - cnt;
+                const int items = __shfl_sync(0xffffffffu, incl, 31);
+                for (int t0 = 0; t0 < items; t0 += 32) {
+                    const int t = t0 + lane;
+                    int o = 0;
+                    #pragma unroll
+                    for (int bit = 16; bit > 0; bit >>= 1) {
+                        const int v = __shfl_sync(0xffffffffu, excl, o + bit);
+                        if (v <= t) o += bit;
+                    }
+                    const int off_o = __shfl_sync(0xffffffffu, excl, o);
+                    const int jlo_o = __shfl_sync(0xffffffffu, jlo, o);
+                    if (t >= items) continue;
+                    const Entry<T> en = ent[e0 + o];
+                    const SlotParams<T> &p = prm[eslot[e0 + o]];
+                    const int j = jlo_o + (t - off_o);
+                    T te = en.te, ne = en.ne;
+                    bool visited = true;
+                    if (j != 0) {
+                        const T dt = j > 0 ? p.ts : -p.ts, dn = j > 0 ? p.ns : -p.ns;
+                        te = A::add(te, dt);
+                        ne = A::add(ne, dn);
+                        visited = fabs(ne) < p.ne_thr;
+                        const int k = j > 0 ? j : -j;
+                        for (int i = 1; i < k; i++) {
+                            te = A::add(te, dt);
+                            ne = A::add(ne, dn);
+                        }
+                        visited = visited && fabs(ne) < p.ne_thr;
+                    }
+                    if (!visited) continue;
+                    const T nf = A::nterm(ne, p);
+                    const T E = A::error(te, nf, p);
+                    if (!(E <= T(1))) continue;
+                    const T v = A::mul(a.max_val, A::template profile<K>(A::sqrt(E)));
+                    const int y = en.sc + j;
+                    T *dst = p.axis ? acc + ((ptrdiff_t)(en.c - y0) * tw + (y - x0))
+                                    : acc + ((ptrdiff_t)(y - y0) * tw + (en.c - x0));
+                    if (OV == CBC_SUM) atomicAdd(dst, v); else combine_max(dst, v);
                 }
             }
         }
         __syncthreads();
     }
 
-    for (int e = threadIdx.x; e < tw * th; e += kThreads) {
-        int r = e / tw, c = e - r * tw;
-        gout[(size_t)r * g.W + c] = tile[e];
+    /* sparse read-modify-write: only pixels that some line drew are read and written;
+     * each thread scans a group of 4 pixels of one tile row per step */
+    T *gout = a.out + ((size_t)frame * g.H + y0) * g.W + x0;
+    const int gpr = (tw + 3) >> 2;                       /* 4-pixel groups per row */
+    for (int q = threadIdx.x; q < gpr * th; q += blockDim.x) {
+        const int r = q / gpr, c = (q - r * gpr) * 4;
+        const T *src = acc + (size_t)r * tw + c;
+        T *dst = gout + (size_t)r * g.W + c;
+        const int m = min(4, tw - c);
+        #pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= m) break;
+            const T v = src[k];
+            if (OV == CBC_SUM) {
+                if (Sentinel<T>::sum_touched(v)) dst[k] = A::add(dst[k], v);
+            } else if (v != T(-INFINITY)) {
+                const T o = dst[k];
+                if (o < v) dst[k] = v;
+            }
+        }
+    }
+}
+
+/* ---- lines strategy ----------------------------------------------------------------
+ * One warp draws 32 lines: every lane walks its own line (bresenham.hpp:352-383 outer
+ * loop) kSegL columns per round into the warp's shared entries, then the warp
+ * flattens the spans of those entries into one pixel per lane and combines each
+ * drawn pixel into `out` with an L2 reduction.  No binning and no workspace beyond
+ * the status block; frame indices and walk ranges are validated by a separate kernel
+ * first, so an invalid call leaves `out` untouched. */
+
+constexpr int kLinesWarps = 4;
+constexpr int kSegL = 8;
+
+template <typename T, typename IdxT>
+__global__ void __launch_bounds__(kThreads)
+validate_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
+                long long n_frames, DevStatus *st)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n_lines;
+    long long frame = 0;
+    const bool has_idx = idxs != nullptr;
+    if (in) frame = has_idx ? load_idx<IdxT>(idxs, i) : (n_frames == 1 ? 0 : i);
+    if (has_idx) warp_minmax(frame, in, st);
+    if (!in) return;
+    if (frame < 0 || frame >= n_frames) {
+        atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
+        atomicMin(&st->bad_line, (unsigned long long)i);
+        return;
+    }
+    LineRec<T> r;
+    bool too_long = false;
+    if (!build_rec(lines + 5 * i, r, too_long) && too_long) {
+        atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+        atomicMin(&st->bad_line, (unsigned long long)i);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void global_combine_max(T *addr, T v);
+
+template <>
+__device__ __forceinline__ void global_combine_max<float>(float *addr, float v)
+{
+    if (v > 0.0f) {
+        /* positive v: the integer order of the bit patterns is std::max's order for
+         * every out except a negative-signed NaN */
+        atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+    } else if (v == v) {
+        combine_max(addr, v);
+    }
+}
+
+template <>
+__device__ __forceinline__ void global_combine_max<double>(double *addr, double v)
+{
+    if (v > 0.0) {
+        atomicMax(reinterpret_cast<long long *>(addr), __double_as_longlong(v));
+    } else if (v == v) {
+        combine_max(addr, v);
+    }
+}
+
+template <typename T>
+struct LinesArgs {
+    T *out;
+    const T *lines;
+    const void *idxs;
+    long long n_lines, n_frames;
+    int H, W;
+    T max_val;
+    DevStatus *st;
+};
+
+template <typename T, typename IdxT, int K, int OV>
+__global__ void __launch_bounds__(kLinesWarps * 32)
+lines_kernel(LinesArgs<T> a)
+{
+    using A = Ar<T>;
+    __shared__ Entry<T> ent_s[kLinesWarps][32 * kSegL];
+    __shared__ SlotParams<T> prm_s[kLinesWarps][32];
+    __shared__ long long fbase_s[kLinesWarps][32];
+    if (a.st->flags & kFatal) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Entry<T> *ent = ent_s[warp];
+    SlotParams<T> *prm = prm_s[warp];
+    long long *fbase = fbase_s[warp];
+    const long long i = ((long long)blockIdx.x * kLinesWarps + warp) * 32 + lane;
+
+    Geometry g;
+    g.H = a.H;
+    g.W = a.W;
+    g.tile_w = g.tile_h = 1;
+    g.tiles_x = g.tiles_y = 1;
+    LineRec<T> r;
+    Coverage<T> cv;
+    Walker<T> wk;
+    bool done = true;
+    int ax = 0, c0 = 0, sa = 1, ncols = 0;
+    if (i < a.n_lines) {
+        long long frame = a.idxs ? load_idx<IdxT>(a.idxs, i) : (a.n_frames == 1 ? 0 : i);
+        bool too_long = false;
+        if (build_rec(a.lines + 5 * i, r, too_long) && cv.init(r, g)) {
+            done = false;
+            ax = cv.a;
+            sa = cv.sa;
+            c0 = sa > 0 ? cv.lmin : cv.lmax;
+            ncols = cv.lmax - cv.lmin + 1;
+            wk.init(r);
+            wk.cx = r.x0;
+            wk.cy = r.y0;
+            wk.te = r.te0;
+            wk.ne = r.ne0;
+            SlotParams<T> p;
+            p.ts = ax ? r.t0 : r.t1;
+            p.ns = ax ? r.t1 : -r.t0;
+            p.len = r.len;
+            p.len2 = r.len2;
+            p.ww = r.ww;
+            p.rlen = r.rlen;
+            p.rww = r.rww;
+            p.ne_thr = r.ne_thr;
+            p.ss = ax ? wk.sx : wk.sy;
+            p.axis = ax;
+            p.fast = (r.flags & kFastDiv) ? 1 : 0;
+            prm[lane] = p;
+            fbase[lane] = frame * (long long)a.H * a.W;
+        }
+    }
+    int rs = 0;
+    long long guard = 0;
+    while (__any_sync(0xffffffffu, !done)) {
+        #pragma unroll
+        for (int k = 0; k < kSegL; k++) ent[lane * kSegL + k].c = kInvalidEntry;
+        if (!done) {
+            /* walk indices [rs, re] of this round, never past the frame's last column */
+            const int re = min(rs + kSegL - 1, ncols - 1);
+            for (;;) {
+                if (wk.cx == r.x1 || wk.cy == r.y1) { done = true; break; }
+                bool nx, ny;
+                T exx;
+                wk.decide(nx, ny, exx);
+                const int c = ax ? wk.cy : wk.cx;
+                const int idx = (c - c0) * sa;
+                if (idx > re) break;
+                if ((ax ? ny : nx) && idx >= rs) {
+                    Entry<T> en;
+                    en.c = c;
+                    en.sc = ax ? wk.cx : wk.cy;
+                    en.te = wk.te;
+                    en.ne = wk.ne;
+                    ent[lane * kSegL + (idx - rs)] = en;
+                }
+                wk.step(nx, ny, exx);
+                if (++guard > 4LL * CBC_MAX_WALK + 64) {
+                    atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                    done = true;
+                    break;
+                }
+            }
+            if (re >= ncols - 1) done = true;
+        }
+        __syncwarp();
+        #pragma unroll 1
+        for (int b = 0; b < kSegL; b++) {
+            const int e = b * 32 + lane;
+            int cnt = 0, jlo = 0;
+            {
+                const Entry<T> en = ent[e];
+                if (en.c != kInvalidEntry) {
+                    const SlotParams<T> &p = prm[e / kSegL];
+                    const int s_hi = (p.axis ? a.W : a.H) - 1;
+                    const float reach = ((float)p.ne_thr + fabsf((float)en.ne)) / fabsf((float)p.ns);
+                    const int J = reach < 2e9f ? (int)reach + 2 : INT_MAX / 4;
+                    jlo = max(-J, -en.sc);
+                    const int jhi = min(J, s_hi - en.sc);
+                    cnt = max(0, jhi - jlo + 1);
+                }
+            }
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            const int excl = incl - cnt;
+            const int items = __shfl_sync(0xffffffffu, incl, 31);
+            for (int t0 = 0; t0 < items; t0 += 32) {
+                const int t = t0 + lane;
+                int o = 0;
+                #pragma unroll
+                for (int bit = 16; bit > 0; bit >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, excl, o + bit);
+                    if (v <= t) o += bit;
+                }
+                const int off_o = __shfl_sync(0xffffffffu, excl, o);
+                const int jlo_o = __shfl_sync(0xffffffffu, jlo, o);
+                if (t >= items) continue;
+                const int eo = b * 32 + o;
+                const Entry<T> en = ent[eo];
+                const SlotParams<T> &p = prm[eo / kSegL];
+                const int j = jlo_o + (t - off_o);
+                T te = en.te, ne = en.ne;
+                bool visited = true;
+                if (j != 0) {
+                    const T dt = j > 0 ? p.ts : -p.ts, dn = j > 0 ? p.ns : -p.ns;
+                    te = A::add(te, dt);
+                    ne = A::add(ne, dn);
+                    visited = fabs(ne) < p.ne_thr;
+                    const int k = j > 0 ? j : -j;
+                    for (int q = 1; q < k; q++) {
+                        te = A::add(te, dt);
+                        ne = A::add(ne, dn);
+                    }
+                    visited = visited && fabs(ne) < p.ne_thr;
+                }
+                if (!visited) continue;
+                const T nf = A::nterm(ne, p);
+                const T E = A::error(te, nf, p);
+                if (!(E <= T(1))) continue;
+                const T v = A::mul(a.max_val, A::template profile<K>(A::sqrt(E)));
+                const int y = en.sc + j;
+                const int px = p.axis ? y : en.c, py = p.axis ? en.c : y;
+                T *dst = a.out + fbase[eo / kSegL] + (long long)py * a.W + px;
+                if (OV == CBC_SUM) atomicAdd(dst, v); else global_combine_max(dst, v);
+            }
+        }
+        __syncwarp();
+        rs += kSegL;
     }
 }
 
@@ -645,13 +1166,13 @@ int fail(int code, const std::string &msg)
 }
 
 struct Layout {
-    size_t status, recs, counts, offsets, fillpos, pairs, total;
+    size_t status, recs, counts, offsets, fillpos, pairs, cks, total;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 struct Resolved {
-    int tile_w, tile_h, chunk, ent_cap;
+    int tile_w, tile_h, chunk, ent_cap, threads, strategy;
 };
 
 bool resolve_tuning(const cbc_tuning *t, Resolved &r, std::string &why)
@@ -659,6 +1180,13 @@ bool resolve_tuning(const cbc_tuning *t, Resolved &r, std::string &why)
     r.tile_w = (t && t->tile_w) ? t->tile_w : kDefaultTileW;
     r.tile_h = (t && t->tile_h) ? t->tile_h : kDefaultTileH;
     r.chunk = (t && t->chunk_lines) ? t->chunk_lines : kDefaultChunk;
+    r.threads = (t && t->threads) ? t->threads : kThreads;
+    r.strategy = t ? t->strategy : CBC_STRATEGY_AUTO;
+    if (r.strategy < CBC_STRATEGY_AUTO || r.strategy > CBC_STRATEGY_LINES) {
+        why = "strategy must be CBC_STRATEGY_AUTO, _TILES or _LINES";
+        return false;
+    }
+    if (r.threads != 128 && r.threads != 256) { why = "threads must be 128 or 256"; return false; }
     if (r.tile_w < 16 || r.tile_w > 256 || (r.tile_w & 3)) { why = "tile_w must be a multiple of 4 in [16, 256]"; return false; }
     if (r.tile_h < 4 || r.tile_h > 256) { why = "tile_h must be in [4, 256]"; return false; }
     if (r.chunk < 1 || r.chunk > kMaxChunk) { why = "chunk_lines must be in [1, 32]"; return false; }
@@ -667,7 +1195,8 @@ bool resolve_tuning(const cbc_tuning *t, Resolved &r, std::string &why)
 }
 
 Layout make_layout(long long n_frames, long long H, long long W, long long n_lines,
-                   long long capacity, size_t rec_bytes, const Resolved &t)
+                   long long capacity, long long ck_capacity, size_t rec_bytes,
+                   size_t ck_bytes, const Resolved &t)
 {
     Layout L;
     long long tiles_x = (W + t.tile_w - 1) / t.tile_w, tiles_y = (H + t.tile_h - 1) / t.tile_h;
@@ -679,12 +1208,14 @@ Layout make_layout(long long n_frames, long long H, long long W, long long n_lin
     L.fillpos = off; off = align_up(off + sizeof(int) * (size_t)n_bins, 256);
     L.recs = off;    off = align_up(off + rec_bytes * (size_t)n_lines, 256);
     L.pairs = off;   off = align_up(off + sizeof(int) * (size_t)capacity, 256);
+    L.cks = off;     off = align_up(off + ck_bytes * (size_t)ck_capacity, 256);
     L.total = off;
     return L;
 }
 
 template <typename T, int K, int OV>
-cudaError_t launch_render(const RenderArgs<T> &ra, long long n_bins, size_t smem, cudaStream_t s)
+cudaError_t launch_render(const RenderArgs<T> &ra, long long n_bins, size_t smem, cudaStream_t s,
+                          int threads)
 {
     auto fn = render_kernel<T, K, OV>;
     if (smem > 48 * 1024) {
@@ -692,36 +1223,67 @@ cudaError_t launch_render(const RenderArgs<T> &ra, long long n_bins, size_t smem
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    fn<<<(unsigned)n_bins, kThreads, smem, s>>>(ra);
+    fn<<<(unsigned)n_bins, threads, smem, s>>>(ra);
     return cudaGetLastError();
 }
 
 template <typename T, int K>
 cudaError_t launch_render_ov(const RenderArgs<T> &ra, int overlap, long long n_bins, size_t smem,
-                             cudaStream_t s)
+                             cudaStream_t s, int threads)
 {
-    return overlap == CBC_MAX ? launch_render<T, K, CBC_MAX>(ra, n_bins, smem, s)
-                              : launch_render<T, K, CBC_SUM>(ra, n_bins, smem, s);
+    return overlap == CBC_MAX ? launch_render<T, K, CBC_MAX>(ra, n_bins, smem, s, threads)
+                              : launch_render<T, K, CBC_SUM>(ra, n_bins, smem, s, threads);
 }
 
 template <typename T>
 cudaError_t launch_render_k(const RenderArgs<T> &ra, int kernel, int overlap, long long n_bins,
-                            size_t smem, cudaStream_t s)
+                            size_t smem, cudaStream_t s, int threads)
 {
     switch (kernel) {
-    case CBC_BIWEIGHT:    return launch_render_ov<T, CBC_BIWEIGHT>(ra, overlap, n_bins, smem, s);
-    case CBC_GAUSSIAN:    return launch_render_ov<T, CBC_GAUSSIAN>(ra, overlap, n_bins, smem, s);
-    case CBC_PARABOLIC:   return launch_render_ov<T, CBC_PARABOLIC>(ra, overlap, n_bins, smem, s);
-    case CBC_RECTANGULAR: return launch_render_ov<T, CBC_RECTANGULAR>(ra, overlap, n_bins, smem, s);
-    default:              return launch_render_ov<T, CBC_TRIANGULAR>(ra, overlap, n_bins, smem, s);
+    case CBC_BIWEIGHT:    return launch_render_ov<T, CBC_BIWEIGHT>(ra, overlap, n_bins, smem, s, threads);
+    case CBC_GAUSSIAN:    return launch_render_ov<T, CBC_GAUSSIAN>(ra, overlap, n_bins, smem, s, threads);
+    case CBC_PARABOLIC:   return launch_render_ov<T, CBC_PARABOLIC>(ra, overlap, n_bins, smem, s, threads);
+    case CBC_RECTANGULAR: return launch_render_ov<T, CBC_RECTANGULAR>(ra, overlap, n_bins, smem, s, threads);
+    default:              return launch_render_ov<T, CBC_TRIANGULAR>(ra, overlap, n_bins, smem, s, threads);
     }
 }
+
+template <typename T, typename IdxT, int K, int OV>
+cudaError_t launch_lines(const LinesArgs<T> &la, cudaStream_t s)
+{
+    const long long per_cta = 32LL * kLinesWarps;
+    lines_kernel<T, IdxT, K, OV><<<(unsigned)((la.n_lines + per_cta - 1) / per_cta),
+                                   kLinesWarps * 32, 0, s>>>(la);
+    return cudaGetLastError();
+}
+
+template <typename T, typename IdxT, int K>
+cudaError_t launch_lines_ov(const LinesArgs<T> &la, int overlap, cudaStream_t s)
+{
+    return overlap == CBC_MAX ? launch_lines<T, IdxT, K, CBC_MAX>(la, s)
+                              : launch_lines<T, IdxT, K, CBC_SUM>(la, s);
+}
+
+template <typename T, typename IdxT>
+cudaError_t launch_lines_k(const LinesArgs<T> &la, int kernel, int overlap, cudaStream_t s)
+{
+    switch (kernel) {
+    case CBC_BIWEIGHT:    return launch_lines_ov<T, IdxT, CBC_BIWEIGHT>(la, overlap, s);
+    case CBC_GAUSSIAN:    return launch_lines_ov<T, IdxT, CBC_GAUSSIAN>(la, overlap, s);
+    case CBC_PARABOLIC:   return launch_lines_ov<T, IdxT, CBC_PARABOLIC>(la, overlap, s);
+    case CBC_RECTANGULAR: return launch_lines_ov<T, IdxT, CBC_RECTANGULAR>(la, overlap, s);
+    default:              return launch_lines_ov<T, IdxT, CBC_TRIANGULAR>(la, overlap, s);
+    }
+}
+
+/* lines per megapixel below which warps of lines beat (frame, tile) bins */
+constexpr double kLinesDensity = 1000.0;
 
 template <typename T>
 int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const T *lines,
                     long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel,
                     int overlap, void *workspace, size_t ws_bytes, long long capacity,
-                    const cbc_tuning *tuning, void *stream)
+                    long long ck_capacity, const cbc_tuning *tuning, void *stream)
 {
     g_error.clear();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
@@ -739,11 +1301,14 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     if (n_lines > 0 && (!out || !lines) && n_frames * H * W > 0)
         return fail(CBC_ERR_INVALID, "null pointer");
     if (capacity < 0 || capacity > INT_MAX) return fail(CBC_ERR_INVALID, "pair_capacity out of range");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
     if (n_lines > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines");
     Resolved t;
     std::string why;
     if (!resolve_tuning(tuning, t, why)) return fail(CBC_ERR_INVALID, why);
-    Layout L = make_layout(n_frames, H, W, n_lines, capacity, sizeof(LineRec<T>), t);
+    Layout L = make_layout(n_frames, H, W, n_lines, capacity, ck_capacity, sizeof(LineRec<T>),
+                           sizeof(Checkpoint<T>), t);
     if (!workspace || ws_bytes < L.total)
         return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
                                          std::to_string(L.total) + ")");
@@ -763,18 +1328,53 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     g.tiles_y = (int)((H + t.tile_h - 1) / t.tile_h);
     long long n_bins = n_frames * (long long)g.tiles_x * g.tiles_y;
     if (n_bins > INT_MAX) return fail(CBC_ERR_INVALID, "too many (frame, tile) bins");
-    int *counts = reinterpret_cast<int *>(ws + L.counts);
-    if (e == cudaSuccess && n_bins > 0) e = cudaMemsetAsync(counts, 0, sizeof(int) * n_bins, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines == 0) return CBC_OK;
-    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
     unsigned nb_lines = (unsigned)((n_lines + kThreads - 1) / kThreads);
+    int strategy = t.strategy;
+    if (strategy == CBC_STRATEGY_AUTO) {
+        double mpx = (double)n_frames * (double)H * (double)W / 1e6;
+        strategy = (mpx > 0.0 && (double)n_lines / mpx < kLinesDensity) ? CBC_STRATEGY_LINES
+                                                                         : CBC_STRATEGY_TILES;
+    }
+    if (strategy == CBC_STRATEGY_LINES) {
+        const bool wide = idxs && idx_bytes == 8;
+        if (wide) validate_kernel<T, int64_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, st);
+        else      validate_kernel<T, int32_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, st);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        timer.mark(1);
+        timer.mark(2);
+        timer.mark(3);
+        if (n_frames * H * W > 0) {
+            LinesArgs<T> la;
+            la.out = out;
+            la.lines = lines;
+            la.idxs = idxs;
+            la.n_lines = n_lines;
+            la.n_frames = n_frames;
+            la.H = (int)H;
+            la.W = (int)W;
+            la.max_val = max_val;
+            la.st = st;
+            e = wide ? launch_lines_k<T, int64_t>(la, kernel, overlap, s)
+                     : launch_lines_k<T, int32_t>(la, kernel, overlap, s);
+            if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        }
+        timer.mark(4);
+        timer.commit();
+        return CBC_OK;
+    }
+    int *counts = reinterpret_cast<int *>(ws + L.counts);
+    if (n_bins > 0) e = cudaMemsetAsync(counts, 0, sizeof(int) * n_bins, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
     if (!idxs || idx_bytes == 4)
         prep_kernel<T, int32_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                              recs, counts, st);
+                                                              recs, counts, ck_capacity, st);
     else
         prep_kernel<T, int64_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                              recs, counts, st);
+                                                              recs, counts, ck_capacity, st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_bins == 0) return CBC_OK;
@@ -782,10 +1382,12 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     int *offsets = reinterpret_cast<int *>(ws + L.offsets);
     int *fillpos = reinterpret_cast<int *>(ws + L.fillpos);
     int *pairs = reinterpret_cast<int *>(ws + L.pairs);
+    Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
     offsets_kernel<<<(unsigned)((n_bins + kThreads - 1) / kThreads), kThreads, 0, s>>>(
         counts, offsets, fillpos, n_bins, capacity, st);
     timer.mark(2);
-    fill_kernel<T><<<nb_lines, kThreads, 0, s>>>(recs, n_lines, g, fillpos, pairs, capacity, st);
+    fill_kernel<T><<<nb_lines, kThreads, 0, s>>>(recs, n_lines, g, fillpos, pairs, capacity, cks,
+                                                 st);
     timer.mark(3);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
@@ -795,13 +1397,14 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     ra.counts = counts;
     ra.offsets = offsets;
     ra.pairs = pairs;
+    ra.cks = cks;
     ra.st = st;
     ra.g = g;
     ra.max_val = max_val;
     ra.chunk = t.chunk;
     ra.ent_cap = t.ent_cap;
     size_t smem = render_smem_bytes<T>(t.tile_w, t.tile_h, t.ent_cap);
-    e = launch_render_k<T>(ra, kernel, overlap, n_bins, smem, s);
+    e = launch_render_k<T>(ra, kernel, overlap, n_bins, smem, s, t.threads);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     timer.mark(4);
     timer.commit();
@@ -813,37 +1416,44 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
 extern "C" {
 
 size_t cbc_draw_lines_workspace_size(int64_t n_frames, int64_t height, int64_t width,
-                                     int64_t n_lines, int64_t pair_capacity, int32_t elem_bytes,
+                                     int64_t n_lines, int64_t pair_capacity,
+                                     int64_t checkpoint_capacity, int32_t elem_bytes,
                                      const cbc_tuning *tuning)
 {
     cbc::Resolved t;
     std::string why;
     if (!cbc::resolve_tuning(tuning, t, why)) return 0;
-    if (n_frames < 0 || height < 0 || width < 0 || n_lines < 0 || pair_capacity < 0) return 0;
+    if (n_frames < 0 || height < 0 || width < 0 || n_lines < 0 || pair_capacity < 0 ||
+        checkpoint_capacity < 0)
+        return 0;
     size_t rec = elem_bytes == 8 ? sizeof(cbc::LineRec<double>) : sizeof(cbc::LineRec<float>);
-    return cbc::make_layout(n_frames, height, width, n_lines, pair_capacity, rec, t).total;
+    size_t ck = elem_bytes == 8 ? sizeof(cbc::Checkpoint<double>) : sizeof(cbc::Checkpoint<float>);
+    return cbc::make_layout(n_frames, height, width, n_lines, pair_capacity, checkpoint_capacity,
+                            rec, ck, t).total;
 }
 
 int cbc_draw_lines_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
                        const float *lines, int64_t n_lines, const void *idxs, int32_t idx_bytes,
                        float max_val, int32_t kernel, int32_t overlap, void *workspace,
-                       size_t workspace_bytes, int64_t pair_capacity, const cbc_tuning *tuning,
-                       void *stream)
+                       size_t workspace_bytes, int64_t pair_capacity,
+                       int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
 {
     return cbc::draw_lines_impl<float>(out, n_frames, height, width, lines, n_lines, idxs,
                                        idx_bytes, max_val, kernel, overlap, workspace,
-                                       workspace_bytes, pair_capacity, tuning, stream);
+                                       workspace_bytes, pair_capacity, checkpoint_capacity,
+                                       tuning, stream);
 }
 
 int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
                        const double *lines, int64_t n_lines, const void *idxs, int32_t idx_bytes,
                        double max_val, int32_t kernel, int32_t overlap, void *workspace,
-                       size_t workspace_bytes, int64_t pair_capacity, const cbc_tuning *tuning,
-                       void *stream)
+                       size_t workspace_bytes, int64_t pair_capacity,
+                       int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
 {
     return cbc::draw_lines_impl<double>(out, n_frames, height, width, lines, n_lines, idxs,
                                         idx_bytes, max_val, kernel, overlap, workspace,
-                                        workspace_bytes, pair_capacity, tuning, stream);
+                                        workspace_bytes, pair_capacity, checkpoint_capacity,
+                                        tuning, stream);
 }
 
 int cbc_read_status(const void *workspace, cbc_status *status, void *stream)
@@ -861,6 +1471,7 @@ int cbc_read_status(const void *workspace, cbc_status *status, void *stream)
     status->idx_min = d.idx_min;
     status->idx_max = d.idx_max;
     status->pairs_needed = (int64_t)d.pairs;
+    status->checkpoints_needed = (int64_t)d.cks;
     return CBC_OK;
 }
 

@@ -6,9 +6,10 @@ Same signature, argument meaning and error behaviour as the reference's public o
 path bit for bit (max overlap, and sum apart from the order in which several lines'
 contributions to one pixel are added).
 """
+import contextlib
 import math
 import threading
-from typing import Optional, Tuple
+from typing import Iterator, Optional, Tuple
 
 import numpy as np
 import torch
@@ -16,7 +17,26 @@ import torch
 from . import _native
 from . import device as _device
 
-__all__ = ['draw_lines', 'Workspace']
+__all__ = ['draw_lines', 'Workspace', 'tuning']
+
+_tls = threading.local()
+
+
+@contextlib.contextmanager
+def tuning(**fields) -> Iterator[_native.Tuning]:
+    """Force render settings (cbc_tuning fields: tile_w, tile_h, chunk_lines, threads,
+    strategy) for the draw_lines calls of this thread inside the block."""
+    t = _native.Tuning()
+    for k, v in fields.items():
+        if not hasattr(t, k):
+            raise AttributeError(f"cbc_tuning has no field {k!r}")
+        setattr(t, k, int(v))
+    prev = getattr(_tls, 'tuning', None)
+    _tls.tuning = t
+    try:
+        yield t
+    finally:
+        _tls.tuning = prev
 
 
 class Workspace:
@@ -29,6 +49,7 @@ class Workspace:
         self.device = dev
         self.buffer: Optional[torch.Tensor] = None
         self.capacity = 0
+        self.ck_capacity = 0
 
     def ensure(self, nbytes: int) -> torch.Tensor:
         if self.buffer is None or self.buffer.numel() < nbytes:
@@ -104,6 +125,8 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
                      overlap: int, tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
     if out.dtype not in (torch.float32, torch.float64):
         raise TypeError(f"out must be float32 or float64, got {out.dtype}")
+    if tuning is None:
+        tuning = getattr(_tls, 'tuning', None)
     if out.dim() < 2:
         raise ValueError("Output array has insufficient number of dimensions")
     dev = out.device
@@ -122,16 +145,19 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
         stream = torch.cuda.current_stream(dev)
         ws = _workspace(dev, stream)
         capacity = max(ws.capacity, 4 * n_lines + 1024)
+        ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
         tref = None if tuning is None else ctypes_pointer(tuning)
         for _ in range(4):
-            nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity, elem, tref)
+            nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity, ck_capacity,
+                                                       elem, tref)
             if nbytes == 0:
                 raise ValueError(_native.last_error() or "invalid sizes or tuning")
             buf = ws.ensure(nbytes)
             rc = fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines,
                     None if ix is None else ix.data_ptr(),
                     0 if ix is None else ix.element_size(), max_val, kernel, overlap,
-                    buf.data_ptr(), buf.numel(), capacity, tref, stream.cuda_stream)
+                    buf.data_ptr(), buf.numel(), capacity, ck_capacity, tref,
+                    stream.cuda_stream)
             if rc:
                 _raise_rc(rc)
             st = _native.Status()
@@ -141,10 +167,12 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
             _raise_status(st, F)
             if not st.has(_native.CBC_ERR_CAPACITY):
                 ws.capacity = capacity
+                ws.ck_capacity = ck_capacity
                 break
-            capacity = int(st.pairs_needed * 1.25) + 1024
-            if capacity > 2**31 - 1:
-                raise MemoryError("too many (line, tile) pairs for one call")
+            capacity = max(capacity, int(st.pairs_needed * 1.25) + 1024)
+            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
+            if capacity > 2**31 - 1 or ck_capacity > 2**31 - 1:
+                raise MemoryError("too many (line, tile) pairs or walk checkpoints for one call")
         else:
             raise RuntimeError("pair capacity did not converge")
     if work is not out:

@@ -51,11 +51,18 @@ extern "C" {
 #define CBC_SUM 0
 #define CBC_MAX 1
 
-/* tile shape of the render pass; zeros select the built-in default */
+/* render strategies */
+#define CBC_STRATEGY_AUTO  0   /* pick by line density                                  */
+#define CBC_STRATEGY_TILES 1   /* (frame, tile) bins, shared-memory tiles, one pass out */
+#define CBC_STRATEGY_LINES 2   /* warps of 32 lines, L2 reductions into out             */
+
+/* render configuration; zeros select the built-in defaults */
 typedef struct cbc_tuning {
     int32_t tile_w;        /* tile width in pixels (x), multiple of 4, 16..256        */
     int32_t tile_h;        /* tile height in pixels (y), 4..256                       */
     int32_t chunk_lines;   /* lines staged per shared-memory chunk, 1..32             */
+    int32_t threads;       /* threads per render CTA: 128 or 256                      */
+    int32_t strategy;      /* CBC_STRATEGY_*                                          */
     int32_t reserved;
 } cbc_tuning;
 
@@ -67,15 +74,18 @@ typedef struct cbc_status {
     int64_t idx_min;       /* smallest frame index in idxs (INT64_MAX if none)        */
     int64_t idx_max;       /* largest frame index in idxs (INT64_MIN if none)         */
     int64_t pairs_needed;  /* (line, tile) pairs the call produced                    */
+    int64_t checkpoints_needed; /* walk checkpoints the call produced                 */
 } cbc_status;
 
 /* Bytes of device workspace a call with these sizes needs.  `pair_capacity` bounds
- * the (line, tile) pairs; when a call produces more, it draws nothing, sets
- * CBC_ERR_CAPACITY and reports the count in pairs_needed, so the caller can grow the
- * workspace and repeat the call. */
+ * the (line, tile) pairs and `checkpoint_capacity` the walk checkpoints (one per 8
+ * columns of each line's walk inside its frame); when a call produces more of
+ * either, it draws nothing, sets CBC_ERR_CAPACITY and reports both counts, so the
+ * caller can grow the workspace and repeat the call. */
 CBC_API size_t cbc_draw_lines_workspace_size(int64_t n_frames, int64_t height, int64_t width,
-                                     int64_t n_lines, int64_t pair_capacity,
-                                     int32_t elem_bytes, const cbc_tuning *tuning);
+                                             int64_t n_lines, int64_t pair_capacity,
+                                             int64_t checkpoint_capacity, int32_t elem_bytes,
+                                             const cbc_tuning *tuning);
 
 /* draw_lines: out[(f, y, x)] = out ⊕ max_val·K(d/w) for every pixel the reference's
  * Bresenham walk of each line visits with error <= 1, ⊕ = + (CBC_SUM) or max (CBC_MAX).
@@ -88,16 +98,18 @@ CBC_API size_t cbc_draw_lines_workspace_size(int64_t n_frames, int64_t height, i
  * of range, capacity, walk range) are left in the workspace status and leave `out`
  * untouched. */
 CBC_API int cbc_draw_lines_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
-                       const float *lines, int64_t n_lines, const void *idxs,
-                       int32_t idx_bytes, float max_val, int32_t kernel, int32_t overlap,
-                       void *workspace, size_t workspace_bytes, int64_t pair_capacity,
-                       const cbc_tuning *tuning, void *stream);
+                               const float *lines, int64_t n_lines, const void *idxs,
+                               int32_t idx_bytes, float max_val, int32_t kernel,
+                               int32_t overlap, void *workspace, size_t workspace_bytes,
+                               int64_t pair_capacity, int64_t checkpoint_capacity,
+                               const cbc_tuning *tuning, void *stream);
 
 CBC_API int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
-                       const double *lines, int64_t n_lines, const void *idxs,
-                       int32_t idx_bytes, double max_val, int32_t kernel, int32_t overlap,
-                       void *workspace, size_t workspace_bytes, int64_t pair_capacity,
-                       const cbc_tuning *tuning, void *stream);
+                               const double *lines, int64_t n_lines, const void *idxs,
+                               int32_t idx_bytes, double max_val, int32_t kernel,
+                               int32_t overlap, void *workspace, size_t workspace_bytes,
+                               int64_t pair_capacity, int64_t checkpoint_capacity,
+                               const cbc_tuning *tuning, void *stream);
 
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */

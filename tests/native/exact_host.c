@@ -34,3 +34,24 @@ void exact_fast_path_stats(int which, const float *x, int64_t n, int64_t *slow)
     }
     *slow = s;
 }
+
+/* the reciprocal-based division path used when len and ww are in [2^-60, 2^60] */
+void exact_pixel_error_r_batch(const float *te, const float *ne, const float *len,
+                               const float *width, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) {
+        float w = width[i], l = len[i];
+        float ww = w * w, rl = 1.0f / l, rww = 1.0f / ww;
+        if (!(w > 0.0f) || !(l >= CBC_DIV_LO && l <= CBC_DIV_HI && ww >= CBC_DIV_LO && ww <= CBC_DIV_HI)) {
+            out[i] = -1.0f;   /* not a fast-path input */
+            continue;
+        }
+        float nf = cbc_normal_term_r(ne[i], l, rl);
+        out[i] = cbc_pixel_error_r(te[i], nf, l, l * l, ww, rl, rww);
+    }
+}
+
+void exact_div_batch(const float *a, const float *b, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) out[i] = cbc_div(a[i], b[i], 1.0f / b[i]);
+}

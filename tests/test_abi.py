@@ -36,13 +36,14 @@ def test_version():
 
 def test_workspace_size():
     lib = _native.lib()
-    a = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 400000, 4, None)
-    b = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 800000, 4, None)
-    c = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 400000, 8, None)
-    assert 0 < a < b and a < c
-    assert b - a >= 4 * 400000
+    a = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 400000, 900000, 4, None)
+    b = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 800000, 900000, 4, None)
+    c = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 400000, 900000, 8, None)
+    d = lib.cbc_draw_lines_workspace_size(64, 2167, 2070, 128000, 400000, 1800000, 4, None)
+    assert 0 < a < b and a < c and a < d
+    assert b - a >= 4 * 400000 and d - a >= 16 * 900000
     t = _native.Tuning(7, 64, 16, 0)   # tile_w not a multiple of 4
-    assert lib.cbc_draw_lines_workspace_size(1, 64, 64, 10, 100, 4, ctypes.pointer(t)) == 0
+    assert lib.cbc_draw_lines_workspace_size(1, 64, 64, 10, 100, 100, 4, ctypes.pointer(t)) == 0
 
 
 @pytest.mark.parametrize("args,msg", [
@@ -60,7 +61,7 @@ def test_host_validation(args, msg):
     rc = lib.cbc_draw_lines_f32(p['out'], p['n_frames'], p['H'], p['W'], p['lines'],
                                 p['n_lines'], p['idxs'], p['idx_bytes'], p['max_val'],
                                 p['kernel'], p['overlap'], p['ws'], p['ws_bytes'], p['cap'],
-                                None, None)
+                                p['cap'], None, None)
     assert rc == _native.CBC_ERR_INVALID
     assert msg in _native.last_error()
 
@@ -68,5 +69,5 @@ def test_host_validation(args, msg):
 def test_workspace_too_small_is_rejected():
     lib = _native.lib()
     rc = lib.cbc_draw_lines_f32(None, 1, 10, 10, None, 0, None, 0, 1.0, 0, 0, None, 16, 100,
-                                None, None)
+                                100, None, None)
     assert rc == _native.CBC_ERR_INVALID and 'workspace' in _native.last_error()

@@ -24,6 +24,8 @@ def exact(tmp_path_factory):
     P = ctypes.c_void_p
     lib.exact_profile_batch.argtypes = [ctypes.c_int, P, P, ctypes.c_int64]
     lib.exact_pixel_error_batch.argtypes = [P] * 5 + [ctypes.c_int64]
+    lib.exact_pixel_error_r_batch.argtypes = [P] * 5 + [ctypes.c_int64]
+    lib.exact_div_batch.argtypes = [P] * 3 + [ctypes.c_int64]
     return lib
 
 
@@ -78,6 +80,28 @@ def test_pixel_error_bit_exact(exact, olib, mode):
         te = ((rng.random(m) * 2 - 1) * w * ln).astype(np.float32)
     a = np.empty(m, np.float32)
     b = np.empty(m, np.float32)
+    c = np.empty(m, np.float32)
     olib.cbc_oracle_pixel_error_batch_f32(_p(te), _p(ne), _p(ln), _p(w), _p(a), m)
     exact.exact_pixel_error_batch(_p(te), _p(ne), _p(ln), _p(w), _p(b), m)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    exact.exact_pixel_error_r_batch(_p(te), _p(ne), _p(ln), _p(w), _p(c), m)
+    fast = c != -1.0
+    assert fast.mean() > 0.99
+    assert np.array_equal(a[fast].view(np.uint32), c[fast].view(np.uint32))
+
+
+def test_reciprocal_division(exact):
+    """Markstein's correction from a correctly rounded reciprocal gives the IEEE
+    quotient; outside [2^-60, 2^60] the helper defers to the IEEE division."""
+    rng = np.random.default_rng(17)
+    n = 2_000_000
+    ea = rng.integers(-70, 70, n).astype(np.float32)
+    eb = rng.integers(-59, 59, n).astype(np.float32)
+    a = (rng.uniform(1, 2, n) * 2.0**ea * rng.choice([-1, 1], n)).astype(np.float32)
+    b = (rng.uniform(1, 2, n) * 2.0**eb).astype(np.float32)
+    a[:100] = 0.0
+    got = np.empty(n, np.float32)
+    exact.exact_div_batch(_p(a), _p(b), _p(got), n)
+    want = a / b
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    assert same.all()
