@@ -78,6 +78,8 @@ template <typename T>
 struct Checkpoint {
     int32_t cx, cy;
     T te, ne;
+    int32_t line;   /* owning line                  */
+    int32_t seg;    /* segment index within the line */
 };
 
 /* status block at the start of the workspace */
@@ -89,6 +91,7 @@ struct DevStatus {
     long long idx_max;
     unsigned long long pairs;      /* running pair cursor == pairs_needed */
     unsigned long long cks;        /* running checkpoint cursor            */
+    unsigned long long work;       /* work-item counter of the lines render */
 };
 
 /* per line of the current render chunk */
@@ -98,6 +101,7 @@ struct SlotParams {
     T len, len2, ww;
     T rlen, rww;
     T ne_thr;           /* span continuation threshold on |ne|                         */
+    float rns;          /* ~1 / ns, for the span window estimate only                 */
     int ss;             /* step sign along the short axis (first span half)            */
     int axis;
     int fast;           /* len and ww in the range of the division shortcut            */
@@ -376,11 +380,18 @@ __device__ __forceinline__ void warp_minmax(long long v, bool valid, DevStatus *
     }
 }
 
-template <typename T, typename IdxT>
+template <typename T>
+__device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> &cv,
+                                  Checkpoint<T> *__restrict__ cks, DevStatus *st);
+
+/* COUNT_TILES: count the line's (frame, tile) bins (tiles strategy); WALK: also write
+ * its walk checkpoints here (lines strategy, which needs no bins) */
+template <typename T, typename IdxT, bool COUNT_TILES, bool WALK>
 __global__ void __launch_bounds__(kThreads)
 prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
             long long n_frames, Geometry g, LineRec<T> *__restrict__ recs,
-            int *__restrict__ counts, long long ck_capacity, DevStatus *st)
+            int *__restrict__ counts, Checkpoint<T> *__restrict__ cks, long long ck_capacity,
+            DevStatus *st)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < n_lines;
@@ -429,18 +440,22 @@ prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lon
     if (!in) return;
     if (r.flags & kDrawable) {
         unsigned long long cb = wbase + (unsigned long long)(incl - nck);
-        if (cb + (unsigned long long)nck > (unsigned long long)ck_capacity) {
+        const bool ck_ok = cb + (unsigned long long)nck <= (unsigned long long)ck_capacity;
+        if (!ck_ok) {
             atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
             r.ck_base = 0;
         } else {
             r.ck_base = (int32_t)cb;
         }
-        int *fc = counts + (size_t)frame * g.tiles_x * g.tiles_y;
-        for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
-            int j0, j1;
-            if (!cv.rows(ti, j0, j1)) continue;
-            for (int tj = j0; tj <= j1; tj++) atomicAdd(fc + cv.bin(ti, tj, g), 1);
+        if (COUNT_TILES) {
+            int *fc = counts + (size_t)frame * g.tiles_x * g.tiles_y;
+            for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
+                int j0, j1;
+                if (!cv.rows(ti, j0, j1)) continue;
+                for (int tj = j0; tj <= j1; tj++) atomicAdd(fc + cv.bin(ti, tj, g), 1);
+            }
         }
+        if (WALK && ck_ok) write_checkpoints(r, (int)i, cv, cks, st);
     }
     recs[i] = r;
 }
@@ -454,6 +469,7 @@ __global__ void init_status_kernel(DevStatus *st)
     st->idx_max = LLONG_MIN;
     st->pairs = 0;
     st->cks = 0;
+    st->work = 0;
 }
 
 /* bin offsets: block-local exclusive scan + one atomic per block on the pair cursor */
@@ -493,8 +509,57 @@ offsets_kernel(const int *__restrict__ counts, int *__restrict__ offsets,
     fillpos[b] = o32;
 }
 
-/* one thread per line: write the line id into each of its bins, then walk the line
- * once and store the iterator state every kSeg walk columns inside the frame */
+/* walk line i once and store the iterator state every kSeg walk columns inside the
+ * frame (LineIterator state: position and both errors) */
+template <typename T>
+__device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> &cv,
+                                  Checkpoint<T> *__restrict__ cks, DevStatus *st)
+{
+    Walker<T> wk;
+    wk.init(r);
+    wk.cx = r.x0;
+    wk.cy = r.y0;
+    wk.te = r.te0;
+    wk.ne = r.ne0;
+    const int nck = (r.ncols + kSeg - 1) / kSeg;
+    Checkpoint<T> *ck = cks + r.ck_base;
+    int k = 0;
+    long long guard = 0;
+    while (k < nck && wk.cx != r.x1 && wk.cy != r.y1) {
+        const int idx = ((cv.a ? wk.cy : wk.cx) - r.c0) * cv.sa;
+        while (k < nck && idx >= k * kSeg) {
+            Checkpoint<T> c;
+            c.cx = wk.cx;
+            c.cy = wk.cy;
+            c.te = wk.te;
+            c.ne = wk.ne;
+            c.line = i;
+            c.seg = k;
+            ck[k++] = c;
+        }
+        bool nx, ny;
+        T exx;
+        wk.decide(nx, ny, exx);
+        wk.step(nx, ny, exx);
+        if (++guard > 4LL * CBC_MAX_WALK + 64) {
+            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+            break;
+        }
+    }
+    for (; k < nck; k++) {
+        Checkpoint<T> c;
+        c.cx = INT_MIN;
+        c.cy = 0;
+        c.te = T(0);
+        c.ne = T(0);
+        c.line = i;
+        c.seg = k;
+        ck[k] = c;
+    }
+}
+
+/* tiles strategy: one thread per line writes the line id into each of its bins and
+ * then its walk checkpoints */
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 fill_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
@@ -517,43 +582,23 @@ fill_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
             if (pos < capacity) pairs[pos] = (int)i;
         }
     }
-    Walker<T> wk;
-    wk.init(r);
-    wk.cx = r.x0;
-    wk.cy = r.y0;
-    wk.te = r.te0;
-    wk.ne = r.ne0;
-    const int nck = (r.ncols + kSeg - 1) / kSeg;
-    Checkpoint<T> *ck = cks + r.ck_base;
-    int k = 0;
-    long long guard = 0;
-    while (k < nck && wk.cx != r.x1 && wk.cy != r.y1) {
-        const int idx = ((cv.a ? wk.cy : wk.cx) - r.c0) * cv.sa;
-        while (k < nck && idx >= k * kSeg) {
-            Checkpoint<T> c;
-            c.cx = wk.cx;
-            c.cy = wk.cy;
-            c.te = wk.te;
-            c.ne = wk.ne;
-            ck[k++] = c;
-        }
-        bool nx, ny;
-        T exx;
-        wk.decide(nx, ny, exx);
-        wk.step(nx, ny, exx);
-        if (++guard > 4LL * CBC_MAX_WALK + 64) {
-            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
-            break;
-        }
-    }
-    for (; k < nck; k++) {
-        Checkpoint<T> c;
-        c.cx = INT_MIN;
-        c.cy = 0;
-        c.te = T(0);
-        c.ne = T(0);
-        ck[k] = c;
-    }
+    write_checkpoints(r, (int)i, cv, cks, st);
+}
+
+/* lines strategy: one thread per line writes its walk checkpoints */
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+walk_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
+            Checkpoint<T> *__restrict__ cks, DevStatus *st)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    if (st->flags & kFatal) return;
+    const LineRec<T> r = recs[i];
+    if (!(r.flags & kDrawable)) return;
+    Coverage<T> cv;
+    if (!cv.init(r, g)) return;
+    write_checkpoints(r, (int)i, cv, cks, st);
 }
 
 /* ---- render ---------------------------------------------------------------------- */
@@ -630,6 +675,23 @@ __host__ __device__ constexpr size_t render_smem_bytes(int tile_w, int tile_h, i
            kMaxChunk * sizeof(WalkSlot<T>) + 4 * sizeof(int) + 64;
 }
 
+/* window [jlo, jhi] of short-axis offsets from the centre that the span can reach:
+ * ne moves by ns per step, the span stops once |ne| >= ne_thr (float estimate, one
+ * pixel of margin each side), clipped to the frame / tile range [s_lo, s_hi] */
+template <typename T>
+__device__ __forceinline__ int span_window(const SlotParams<T> &p, int sc, T ne, int s_lo,
+                                           int s_hi, int &jlo)
+{
+    const float R = (float)p.ne_thr * fabsf(p.rns);
+    const float u = (float)ne * p.rns;
+    const float up = R - u, dn = R + u;
+    const int kp = up < 2e9f ? (int)floorf(up) + 1 : INT_MAX / 4;
+    const int km = dn < 2e9f ? (int)floorf(dn) + 1 : INT_MAX / 4;
+    jlo = max(-max(km, 0), s_lo - sc);
+    const int jhi = min(max(kp, 0), s_hi - sc);
+    return max(0, jhi - jlo + 1);
+}
+
 template <typename T, int K, int OV>
 __global__ void __launch_bounds__(kThreads)
 render_kernel(RenderArgs<T> a)
@@ -687,6 +749,7 @@ render_kernel(RenderArgs<T> a)
                 p.rlen = r.rlen;
                 p.rww = r.rww;
                 p.ne_thr = r.ne_thr;
+                p.rns = 1.0f / (float)p.ns;
                 p.ss = ax ? sx : sy;
                 p.axis = ax;
                 p.fast = (r.flags & kFastDiv) ? 1 : 0;
@@ -796,12 +859,7 @@ render_kernel(RenderArgs<T> a)
                     if (en.c != kInvalidEntry) {
                         const SlotParams<T> &p = prm[eslot[e]];
                         const int s_lo = p.axis ? x0 : y0, s_hi = p.axis ? x0 + tw - 1 : y0 + th - 1;
-                        /* conservative reach of the span: |ne| grows by |ns| per step */
-                        const float reach = ((float)p.ne_thr + fabsf((float)en.ne)) / fabsf((float)p.ns);
-                        const int J = reach < 2e9f ? (int)reach + 2 : INT_MAX / 4;
-                        jlo = max(-J, s_lo - en.sc);
-                        const int jhi = min(J, s_hi - en.sc);
-                        cnt = max(0, jhi - jlo + 1);
+                        cnt = span_window(p, en.sc, en.ne, s_lo, s_hi, jlo);
                     }
                 }
                 int incl = cnt;
@@ -878,40 +936,14 @@ render_kernel(RenderArgs<T> a)
 }
 
 /* ---- lines strategy ----------------------------------------------------------------
- * One warp draws 32 lines: every lane walks its own line (bresenham.hpp:352-383 outer
- * loop) kSegL columns per round into the warp's shared entries, then the warp
- * flattens the spans of those entries into one pixel per lane and combines each
- * drawn pixel into `out` with an L2 reduction.  No binning and no workspace beyond
- * the status block; frame indices and walk ranges are validated by a separate kernel
- * first, so an invalid call leaves `out` untouched. */
+ * Work items are (line, kSeg-column segment) pairs, i.e. walk checkpoints.  A warp
+ * takes 32 of them: every lane resumes its line's walk (bresenham.hpp:352-383 outer
+ * loop) from the checkpoint for kSeg columns into the warp's shared entries, then the
+ * warp flattens the spans of those entries into one pixel per lane and combines each
+ * drawn pixel into `out` with an L2 reduction.  Persistent grid over all items; no
+ * binning. */
 
-constexpr int kLinesWarps = 4;
-constexpr int kSegL = 8;
-
-template <typename T, typename IdxT>
-__global__ void __launch_bounds__(kThreads)
-validate_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
-                long long n_frames, DevStatus *st)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = i < n_lines;
-    long long frame = 0;
-    const bool has_idx = idxs != nullptr;
-    if (in) frame = has_idx ? load_idx<IdxT>(idxs, i) : (n_frames == 1 ? 0 : i);
-    if (has_idx) warp_minmax(frame, in, st);
-    if (!in) return;
-    if (frame < 0 || frame >= n_frames) {
-        atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
-        atomicMin(&st->bad_line, (unsigned long long)i);
-        return;
-    }
-    LineRec<T> r;
-    bool too_long = false;
-    if (!build_rec(lines + 5 * i, r, too_long) && too_long) {
-        atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
-        atomicMin(&st->bad_line, (unsigned long long)i);
-    }
-}
+constexpr int kSegWarps = 4;
 
 template <typename T>
 __device__ __forceinline__ void global_combine_max(T *addr, T v);
@@ -939,119 +971,102 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
 }
 
 template <typename T>
-struct LinesArgs {
+struct SegArgs {
     T *out;
-    const T *lines;
-    const void *idxs;
-    long long n_lines, n_frames;
+    const LineRec<T> *recs;
+    const Checkpoint<T> *cks;
     int H, W;
     T max_val;
     DevStatus *st;
+    unsigned long long *work;      /* work-item counter, zeroed before the launch */
 };
 
-template <typename T, typename IdxT, int K, int OV>
-__global__ void __launch_bounds__(kLinesWarps * 32)
-lines_kernel(LinesArgs<T> a)
+template <typename T, int K, int OV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+segments_kernel(SegArgs<T> a)
 {
     using A = Ar<T>;
-    __shared__ Entry<T> ent_s[kLinesWarps][32 * kSegL];
-    __shared__ SlotParams<T> prm_s[kLinesWarps][32];
-    __shared__ long long fbase_s[kLinesWarps][32];
+    __shared__ Entry<T> ent_s[kSegWarps][32 * kSeg];
+    __shared__ SlotParams<T> prm_s[kSegWarps][32];
+    __shared__ long long fbase_s[kSegWarps][32];
     if (a.st->flags & kFatal) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     Entry<T> *ent = ent_s[warp];
     SlotParams<T> *prm = prm_s[warp];
     long long *fbase = fbase_s[warp];
-    const long long i = ((long long)blockIdx.x * kLinesWarps + warp) * 32 + lane;
+    const long long total = (long long)a.st->cks;
 
-    Geometry g;
-    g.H = a.H;
-    g.W = a.W;
-    g.tile_w = g.tile_h = 1;
-    g.tiles_x = g.tiles_y = 1;
-    LineRec<T> r;
-    Coverage<T> cv;
-    Walker<T> wk;
-    bool done = true;
-    int ax = 0, c0 = 0, sa = 1, ncols = 0;
-    if (i < a.n_lines) {
-        long long frame = a.idxs ? load_idx<IdxT>(a.idxs, i) : (a.n_frames == 1 ? 0 : i);
-        bool too_long = false;
-        if (build_rec(a.lines + 5 * i, r, too_long) && cv.init(r, g)) {
-            done = false;
-            ax = cv.a;
-            sa = cv.sa;
-            c0 = sa > 0 ? cv.lmin : cv.lmax;
-            ncols = cv.lmax - cv.lmin + 1;
-            wk.init(r);
-            wk.cx = r.x0;
-            wk.cy = r.y0;
-            wk.te = r.te0;
-            wk.ne = r.ne0;
-            SlotParams<T> p;
-            p.ts = ax ? r.t0 : r.t1;
-            p.ns = ax ? r.t1 : -r.t0;
-            p.len = r.len;
-            p.len2 = r.len2;
-            p.ww = r.ww;
-            p.rlen = r.rlen;
-            p.rww = r.rww;
-            p.ne_thr = r.ne_thr;
-            p.ss = ax ? wk.sx : wk.sy;
-            p.axis = ax;
-            p.fast = (r.flags & kFastDiv) ? 1 : 0;
-            prm[lane] = p;
-            fbase[lane] = frame * (long long)a.H * a.W;
-        }
-    }
-    int rs = 0;
-    long long guard = 0;
-    while (__any_sync(0xffffffffu, !done)) {
+    for (;;) {
+        long long base = 0;
+        if (lane == 0) base = (long long)atomicAdd(a.work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const long long item = base + lane;
         #pragma unroll
-        for (int k = 0; k < kSegL; k++) ent[lane * kSegL + k].c = kInvalidEntry;
-        if (!done) {
-            /* walk indices [rs, re] of this round, never past the frame's last column */
-            const int re = min(rs + kSegL - 1, ncols - 1);
-            for (;;) {
-                if (wk.cx == r.x1 || wk.cy == r.y1) { done = true; break; }
-                bool nx, ny;
-                T exx;
-                wk.decide(nx, ny, exx);
-                const int c = ax ? wk.cy : wk.cx;
-                const int idx = (c - c0) * sa;
-                if (idx > re) break;
-                if ((ax ? ny : nx) && idx >= rs) {
-                    Entry<T> en;
-                    en.c = c;
-                    en.sc = ax ? wk.cx : wk.cy;
-                    en.te = wk.te;
-                    en.ne = wk.ne;
-                    ent[lane * kSegL + (idx - rs)] = en;
-                }
-                wk.step(nx, ny, exx);
-                if (++guard > 4LL * CBC_MAX_WALK + 64) {
-                    atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
-                    done = true;
-                    break;
+        for (int k = 0; k < kSeg; k++) ent[lane * kSeg + k].c = kInvalidEntry;
+        if (item < total) {
+            const Checkpoint<T> ck = a.cks[item];
+            if (ck.cx != INT_MIN) {
+                const LineRec<T> r = a.recs[ck.line];
+                const int ax = r.flags & kAxisY;
+                Walker<T> wk;
+                wk.init(r);
+                wk.cx = ck.cx;
+                wk.cy = ck.cy;
+                wk.te = ck.te;
+                wk.ne = ck.ne;
+                const int sa = ax ? wk.sy : wk.sx;
+                const int lo = ck.seg * kSeg, hi = min(lo + kSeg - 1, r.ncols - 1);
+                SlotParams<T> p;
+                p.ts = ax ? r.t0 : r.t1;
+                p.ns = ax ? r.t1 : -r.t0;
+                p.len = r.len;
+                p.len2 = r.len2;
+                p.ww = r.ww;
+                p.rlen = r.rlen;
+                p.rww = r.rww;
+                p.ne_thr = r.ne_thr;
+                p.rns = 1.0f / (float)p.ns;
+                p.ss = ax ? wk.sx : wk.sy;
+                p.axis = ax;
+                p.fast = (r.flags & kFastDiv) ? 1 : 0;
+                prm[lane] = p;
+                fbase[lane] = (long long)r.frame * a.H * a.W;
+                int guard = 0;
+                while (wk.cx != r.x1 && wk.cy != r.y1) {
+                    bool nx, ny;
+                    T exx;
+                    wk.decide(nx, ny, exx);
+                    const int c = ax ? wk.cy : wk.cx;
+                    const int idx = (c - r.c0) * sa;
+                    if (idx > hi) break;
+                    if ((ax ? ny : nx) && idx >= lo) {
+                        Entry<T> en;
+                        en.c = c;
+                        en.sc = ax ? wk.cx : wk.cy;
+                        en.te = wk.te;
+                        en.ne = wk.ne;
+                        ent[lane * kSeg + (idx - lo)] = en;
+                        if (idx == hi) break;
+                    }
+                    wk.step(nx, ny, exx);
+                    if (++guard > 4 * CBC_MAX_WALK + 64) {
+                        atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                        break;
+                    }
                 }
             }
-            if (re >= ncols - 1) done = true;
         }
         __syncwarp();
         #pragma unroll 1
-        for (int b = 0; b < kSegL; b++) {
+        for (int b = 0; b < kSeg; b++) {
             const int e = b * 32 + lane;
             int cnt = 0, jlo = 0;
             {
                 const Entry<T> en = ent[e];
                 if (en.c != kInvalidEntry) {
-                    const SlotParams<T> &p = prm[e / kSegL];
-                    const int s_hi = (p.axis ? a.W : a.H) - 1;
-                    const float reach = ((float)p.ne_thr + fabsf((float)en.ne)) / fabsf((float)p.ns);
-                    const int J = reach < 2e9f ? (int)reach + 2 : INT_MAX / 4;
-                    jlo = max(-J, -en.sc);
-                    const int jhi = min(J, s_hi - en.sc);
-                    cnt = max(0, jhi - jlo + 1);
+                    const SlotParams<T> &p = prm[e / kSeg];
+                    cnt = span_window(p, en.sc, en.ne, 0, (p.axis ? a.W : a.H) - 1, jlo);
                 }
             }
             int incl = cnt;
@@ -1074,7 +1089,7 @@ lines_kernel(LinesArgs<T> a)
                 if (t >= items) continue;
                 const int eo = b * 32 + o;
                 const Entry<T> en = ent[eo];
-                const SlotParams<T> &p = prm[eo / kSegL];
+                const SlotParams<T> &p = prm[eo / kSeg];
                 const int j = jlo_o + (t - off_o);
                 T te = en.te, ne = en.ne;
                 bool visited = true;
@@ -1097,12 +1112,11 @@ lines_kernel(LinesArgs<T> a)
                 const T v = A::mul(a.max_val, A::template profile<K>(A::sqrt(E)));
                 const int y = en.sc + j;
                 const int px = p.axis ? y : en.c, py = p.axis ? en.c : y;
-                T *dst = a.out + fbase[eo / kSegL] + (long long)py * a.W + px;
+                T *dst = a.out + fbase[eo / kSeg] + (long long)py * a.W + px;
                 if (OV == CBC_SUM) atomicAdd(dst, v); else global_combine_max(dst, v);
             }
         }
         __syncwarp();
-        rs += kSegL;
     }
 }
 
@@ -1248,31 +1262,32 @@ cudaError_t launch_render_k(const RenderArgs<T> &ra, int kernel, int overlap, lo
     }
 }
 
-template <typename T, typename IdxT, int K, int OV>
-cudaError_t launch_lines(const LinesArgs<T> &la, cudaStream_t s)
+template <typename T, int K, int OV>
+cudaError_t launch_segments(const SegArgs<T> &sa, cudaStream_t s)
 {
-    const long long per_cta = 32LL * kLinesWarps;
-    lines_kernel<T, IdxT, K, OV><<<(unsigned)((la.n_lines + per_cta - 1) / per_cta),
-                                   kLinesWarps * 32, 0, s>>>(la);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    segments_kernel<T, K, OV><<<(unsigned)(sms > 0 ? sms * 9 : 1024), kSegWarps * 32, 0, s>>>(sa);
     return cudaGetLastError();
 }
 
-template <typename T, typename IdxT, int K>
-cudaError_t launch_lines_ov(const LinesArgs<T> &la, int overlap, cudaStream_t s)
+template <typename T, int K>
+cudaError_t launch_segments_ov(const SegArgs<T> &sa, int overlap, cudaStream_t s)
 {
-    return overlap == CBC_MAX ? launch_lines<T, IdxT, K, CBC_MAX>(la, s)
-                              : launch_lines<T, IdxT, K, CBC_SUM>(la, s);
+    return overlap == CBC_MAX ? launch_segments<T, K, CBC_MAX>(sa, s)
+                              : launch_segments<T, K, CBC_SUM>(sa, s);
 }
 
-template <typename T, typename IdxT>
-cudaError_t launch_lines_k(const LinesArgs<T> &la, int kernel, int overlap, cudaStream_t s)
+template <typename T>
+cudaError_t launch_segments_k(const SegArgs<T> &sa, int kernel, int overlap, cudaStream_t s)
 {
     switch (kernel) {
-    case CBC_BIWEIGHT:    return launch_lines_ov<T, IdxT, CBC_BIWEIGHT>(la, overlap, s);
-    case CBC_GAUSSIAN:    return launch_lines_ov<T, IdxT, CBC_GAUSSIAN>(la, overlap, s);
-    case CBC_PARABOLIC:   return launch_lines_ov<T, IdxT, CBC_PARABOLIC>(la, overlap, s);
-    case CBC_RECTANGULAR: return launch_lines_ov<T, IdxT, CBC_RECTANGULAR>(la, overlap, s);
-    default:              return launch_lines_ov<T, IdxT, CBC_TRIANGULAR>(la, overlap, s);
+    case CBC_BIWEIGHT:    return launch_segments_ov<T, CBC_BIWEIGHT>(sa, overlap, s);
+    case CBC_GAUSSIAN:    return launch_segments_ov<T, CBC_GAUSSIAN>(sa, overlap, s);
+    case CBC_PARABOLIC:   return launch_segments_ov<T, CBC_PARABOLIC>(sa, overlap, s);
+    case CBC_RECTANGULAR: return launch_segments_ov<T, CBC_RECTANGULAR>(sa, overlap, s);
+    default:              return launch_segments_ov<T, CBC_TRIANGULAR>(sa, overlap, s);
     }
 }
 
@@ -1337,28 +1352,30 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
         strategy = (mpx > 0.0 && (double)n_lines / mpx < kLinesDensity) ? CBC_STRATEGY_LINES
                                                                          : CBC_STRATEGY_TILES;
     }
+    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
+    Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
+    const bool wide = idxs && idx_bytes == 8;
     if (strategy == CBC_STRATEGY_LINES) {
-        const bool wide = idxs && idx_bytes == 8;
-        if (wide) validate_kernel<T, int64_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, st);
-        else      validate_kernel<T, int32_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, st);
+        if (wide) prep_kernel<T, int64_t, false, true><<<nb_lines, kThreads, 0, s>>>(
+                      lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
+        else      prep_kernel<T, int32_t, false, true><<<nb_lines, kThreads, 0, s>>>(
+                      lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         timer.mark(1);
         timer.mark(2);
         timer.mark(3);
         if (n_frames * H * W > 0) {
-            LinesArgs<T> la;
-            la.out = out;
-            la.lines = lines;
-            la.idxs = idxs;
-            la.n_lines = n_lines;
-            la.n_frames = n_frames;
-            la.H = (int)H;
-            la.W = (int)W;
-            la.max_val = max_val;
-            la.st = st;
-            e = wide ? launch_lines_k<T, int64_t>(la, kernel, overlap, s)
-                     : launch_lines_k<T, int32_t>(la, kernel, overlap, s);
+            SegArgs<T> sg;
+            sg.out = out;
+            sg.recs = recs;
+            sg.cks = cks;
+            sg.H = (int)H;
+            sg.W = (int)W;
+            sg.max_val = max_val;
+            sg.st = st;
+            sg.work = &st->work;
+            e = launch_segments_k<T>(sg, kernel, overlap, s);
             if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         }
         timer.mark(4);
@@ -1368,13 +1385,12 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     int *counts = reinterpret_cast<int *>(ws + L.counts);
     if (n_bins > 0) e = cudaMemsetAsync(counts, 0, sizeof(int) * n_bins, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
-    if (!idxs || idx_bytes == 4)
-        prep_kernel<T, int32_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                              recs, counts, ck_capacity, st);
+    if (!wide)
+        prep_kernel<T, int32_t, true, false><<<nb_lines, kThreads, 0, s>>>(
+            lines, idxs, n_lines, n_frames, g, recs, counts, cks, ck_capacity, st);
     else
-        prep_kernel<T, int64_t><<<nb_lines, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                              recs, counts, ck_capacity, st);
+        prep_kernel<T, int64_t, true, false><<<nb_lines, kThreads, 0, s>>>(
+            lines, idxs, n_lines, n_frames, g, recs, counts, cks, ck_capacity, st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_bins == 0) return CBC_OK;
@@ -1382,7 +1398,6 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     int *offsets = reinterpret_cast<int *>(ws + L.offsets);
     int *fillpos = reinterpret_cast<int *>(ws + L.fillpos);
     int *pairs = reinterpret_cast<int *>(ws + L.pairs);
-    Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
     offsets_kernel<<<(unsigned)((n_bins + kThreads - 1) / kThreads), kThreads, 0, s>>>(
         counts, offsets, fillpos, n_bins, capacity, st);
     timer.mark(2);
