@@ -1535,3 +1535,135 @@ const char *cbc_last_error(void) { return cbc::g_error.c_str(); }
 const char *cbc_version(void) { return CBC_VERSION; }
 
 }  // extern "C"
+
+/* ---- no-allocation entry point ---------------------------------------------------
+ * The lines-strategy kernels with their scratch (status block, line records, walk
+ * checkpoints) in one fixed device array of this file instead of a caller workspace. */
+
+namespace cbc {
+
+constexpr size_t kNoallocRecOffset = 256;
+constexpr size_t kNoallocCkOffset =
+    kNoallocRecOffset + (sizeof(LineRec<float>) * CBC_NOALLOC_MAX_LINES + 255) / 256 * 256;
+constexpr size_t kNoallocBytes =
+    kNoallocCkOffset + sizeof(Checkpoint<float>) * CBC_NOALLOC_MAX_CHECKPOINTS;
+static_assert(sizeof(DevStatus) <= kNoallocRecOffset, "status block exceeds its slot");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+/* the array's address on the current device, looked up once per device */
+int noalloc_scratch(unsigned char **base)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoallocMaxDevices)
+        return fail(CBC_ERR_INVALID, "device ordinal beyond the no-allocation table");
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(CBC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    return CBC_OK;
+}
+
+int draw_lines_noalloc(float *out, long long n_frames, long long H, long long W,
+                       const float *lines, long long n_lines, const void *idxs, int idx_bytes,
+                       float max_val, int kernel, int overlap, void *stream)
+{
+    g_error.clear();
+    if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (H > INT_MAX / 2 || W > INT_MAX / 2)
+        return fail(CBC_ERR_INVALID, "frame dimensions must be below 2^30");
+    if (kernel < 0 || kernel > 4) return fail(CBC_ERR_INVALID, "Invalid kernel type");
+    if (overlap != CBC_SUM && overlap != CBC_MAX)
+        return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if (idxs && idx_bytes != 4 && idx_bytes != 8)
+        return fail(CBC_ERR_INVALID, "idx_bytes must be 4 or 8");
+    if (!idxs && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
+        return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
+                                         " != " + std::to_string(n_frames) + ")");
+    if (n_lines > CBC_NOALLOC_MAX_LINES)
+        return fail(CBC_ERR_INVALID, "n_lines " + std::to_string(n_lines) +
+                                         " exceeds the no-allocation maximum of " +
+                                         std::to_string(CBC_NOALLOC_MAX_LINES));
+    if (n_lines > 0 && (!out || !lines) && n_frames * H * W > 0)
+        return fail(CBC_ERR_INVALID, "null pointer");
+    unsigned char *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc != CBC_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DevStatus *st = reinterpret_cast<DevStatus *>(base);
+    LineRec<float> *recs = reinterpret_cast<LineRec<float> *>(base + kNoallocRecOffset);
+    Checkpoint<float> *cks = reinterpret_cast<Checkpoint<float> *>(base + kNoallocCkOffset);
+    init_status_kernel<<<1, 1, 0, s>>>(st);        /* every call starts from a clean status */
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines > 0) {
+        Geometry g;
+        g.H = (int)H;
+        g.W = (int)W;
+        g.tile_w = g.tile_h = kDefaultTileW;
+        g.tiles_x = g.tiles_y = 1;
+        const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
+        if (idxs && idx_bytes == 8)
+            prep_kernel<float, int64_t, false, true><<<nb, kThreads, 0, s>>>(
+                lines, idxs, n_lines, n_frames, g, recs, nullptr, cks,
+                CBC_NOALLOC_MAX_CHECKPOINTS, st);
+        else
+            prep_kernel<float, int32_t, false, true><<<nb, kThreads, 0, s>>>(
+                lines, idxs, n_lines, n_frames, g, recs, nullptr, cks,
+                CBC_NOALLOC_MAX_CHECKPOINTS, st);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        if (n_frames * H * W > 0) {
+            SegArgs<float> sg;
+            sg.out = out;
+            sg.recs = recs;
+            sg.cks = cks;
+            sg.H = (int)H;
+            sg.W = (int)W;
+            sg.max_val = max_val;
+            sg.st = st;
+            sg.work = &st->work;
+            e = launch_segments_k<float>(sg, kernel, overlap, s);
+            if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    DevStatus hs;
+    e = cudaMemcpyAsync(&hs, st, sizeof hs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (hs.flags & (1 << CBC_ERR_INDEX))
+        return fail(CBC_ERR_INDEX, "idxs range (" + std::to_string(hs.idx_min) + ", " +
+                                       std::to_string(hs.idx_max) + ") is outside of (0, " +
+                                       std::to_string(n_frames) + ")");
+    if (hs.flags & (1 << CBC_ERR_RANGE))
+        return fail(CBC_ERR_RANGE, "line " + std::to_string(hs.bad_line) +
+                                       ": its walk is longer than CBC_MAX_WALK pixels");
+    if (hs.flags & (1 << CBC_ERR_CAPACITY))
+        return fail(CBC_ERR_CAPACITY, "the walks need " + std::to_string(hs.cks) +
+                                          " checkpoints, more than the no-allocation maximum of " +
+                                          std::to_string(CBC_NOALLOC_MAX_CHECKPOINTS));
+    return CBC_OK;
+}
+
+}  // namespace cbc
+
+extern "C" int cbc_draw_lines_f32_noalloc(float *out, int64_t n_frames, int64_t height,
+                                          int64_t width, const float *lines, int64_t n_lines,
+                                          const void *idxs, int32_t idx_bytes, float max_val,
+                                          int32_t kernel, int32_t overlap, void *stream)
+{
+    return cbc::draw_lines_noalloc(out, n_frames, height, width, lines, n_lines, idxs, idx_bytes,
+                                   max_val, kernel, overlap, stream);
+}

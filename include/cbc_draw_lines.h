@@ -111,6 +111,37 @@ CBC_API int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, in
                                int64_t pair_capacity, int64_t checkpoint_capacity,
                                const cbc_tuning *tuning, void *stream);
 
+/* Limits of cbc_draw_lines_f32_noalloc. */
+#define CBC_NOALLOC_MAX_LINES       16384
+#define CBC_NOALLOC_MAX_CHECKPOINTS 262144
+
+/* cbc_draw_lines_f32 without any device allocation by the caller (no counterpart in
+ * the reference, whose GPU path allocates on every call).
+ *
+ * Some callers cannot hand this library a workspace: a detector acquisition loop
+ * that reserves its whole device memory budget before a run and must not stall on
+ * cudaMalloc's implicit device synchronisation or fail half-way through a run when
+ * memory is short, or a plugin hosted by a framework whose pool allocator owns every
+ * byte of the device.  This entry point needs no memory from them: its scratch is one
+ * fixed array inside the library, about 7.9 MB, held on every GPU that loads the
+ * library until the process exits.
+ *
+ * Arguments and results are those of cbc_draw_lines_f32 (float32 only), with these
+ * limits: n_lines <= CBC_NOALLOC_MAX_LINES, else CBC_ERR_INVALID before any work; and
+ * the lines' walks inside their frames may need at most CBC_NOALLOC_MAX_CHECKPOINTS
+ * checkpoints (one per 8 columns of each walk), else the call draws nothing and
+ * returns CBC_ERR_CAPACITY.  The call waits for `stream` and returns the call's full
+ * status (CBC_OK, CBC_ERR_INDEX, CBC_ERR_CAPACITY, CBC_ERR_RANGE, ...; message in
+ * cbc_last_error).  The first call on each device looks up the array's device
+ * address with that device current; make that first call before any stream capture.
+ * All calls share the one array and every call re-initialises it, so calls that
+ * overlap on the GPU (unordered streams, or threads without ordering) race: issue
+ * them one after another. */
+CBC_API int cbc_draw_lines_f32_noalloc(float *out, int64_t n_frames, int64_t height,
+                                       int64_t width, const float *lines, int64_t n_lines,
+                                       const void *idxs, int32_t idx_bytes, float max_val,
+                                       int32_t kernel, int32_t overlap, void *stream);
+
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
 CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
