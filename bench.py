@@ -45,6 +45,10 @@ def parse():
                    help='frames in the bounded CPU-baseline sample')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--workload', default='detector_stack',
+                   choices=['detector_stack', 'fit'],
+                   help='detector_stack: the headline forward; fit: forward + adjoint '
+                        'iterations on 8 x 1024^2 frames vs a finite-difference gradient')
     return p.parse_args()
 
 
@@ -181,9 +185,77 @@ def workload_config(ls):
             'l2': 'output frames (%.2f GB) exceed L2; no flush' % (F * H * W * 4 / 1e9)}
 
 
+def run_fit(args, world, rank, local):
+    """forward + loss + adjoint iterations/s on the 8 x 1024^2 workload, next to the
+    cost of a finite-difference gradient from the plain forward (2 forwards per
+    parameter, 5 parameters per line)"""
+    import torch
+    from cbclib_v2_gb300 import _native, autograd, draw_lines, workloads
+    torch.cuda.set_device(local)
+    ls = workloads.fit_stack(seed=2000 + rank)
+    truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+    target = torch.zeros(ls.shape, device='cuda')
+    draw_lines(target, workloads.perturbed(ls.lines, 7).astype(np.float32), ls.idxs,
+               ls.max_val, ls.kernel, ls.overlap)
+    gen = torch.Generator(device='cuda').manual_seed(3)
+    target = torch.poisson(target, generator=gen)
+    params = truth.clone().requires_grad_(True)
+
+    def step():
+        img = autograd.draw_lines_fn(params, idxs, shape=ls.shape, max_val=ls.max_val,
+                                     kernel=ls.kernel, overlap=ls.overlap)
+        loss = ((img - target) ** 2).sum()
+        params.grad = None
+        loss.backward()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        loss = step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms_iter = a.elapsed_time(b) / args.steps
+    # one plain forward, the unit of a finite-difference gradient
+    out = torch.zeros(ls.shape, device='cuda')
+    for _ in range(3):
+        out.zero_()
+        draw_lines(out, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(args.steps):
+        out.zero_()
+        draw_lines(out, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms_fwd = a.elapsed_time(b) / args.steps
+    fd_ms = 2 * 5 * ls.n_lines * ms_fwd
+    if rank == 0:
+        print(json.dumps({
+            'metric': 'forward+adjoint iterations/s', 'value': 1e3 / ms_iter * world,
+            'unit': 'iter/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms_iter, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+                       'kernel': ls.kernel, 'overlap': ls.overlap,
+                       'loss': 'sum((I - target)^2), target = Poisson(render(perturbed))'},
+            'forward_ms': ms_fwd,
+            'finite_difference_gradient_ms': fd_ms,
+            'speedup_vs_finite_difference': fd_ms / ms_iter,
+            'loss': float(loss.item())}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
+    if args.workload == 'fit' and args.impl == 'gb300':
+        run_fit(args, world, rank, local)
+        return
     import torch
     from cbclib_v2_gb300 import _native, draw_lines, workloads
 

@@ -48,8 +48,11 @@ _lib = None
 
 # every symbol declared in include/cbc_draw_lines.h
 EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_lines_f64',
-           'cbc_draw_lines_f32_noalloc', 'cbc_read_status', 'cbc_profile_enable',
-           'cbc_profile_read', 'cbc_last_error', 'cbc_version')
+           'cbc_draw_lines_f32_noalloc', 'cbc_draw_lines_backward_workspace_size',
+           'cbc_draw_lines_backward_f32', 'cbc_draw_lines_backward_f64', 'cbc_read_status',
+           'cbc_profile_enable', 'cbc_profile_read', 'cbc_last_error', 'cbc_version')
+
+NO_WINNER = 0x7f7f7f7f
 
 NOALLOC_MAX_LINES = 16384
 NOALLOC_MAX_CHECKPOINTS = 262144
@@ -68,6 +71,13 @@ def _declare(lib):
     lib.cbc_draw_lines_f32_noalloc.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
                                                i32, i32, p]
     lib.cbc_draw_lines_f32_noalloc.restype = ctypes.c_int
+    lib.cbc_draw_lines_backward_workspace_size.argtypes = [i64, i64, i32]
+    lib.cbc_draw_lines_backward_workspace_size.restype = ctypes.c_size_t
+    for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
+        f = getattr(lib, 'cbc_draw_lines_backward_' + sfx)
+        f.argtypes = [p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, p, p, p, p,
+                      ctypes.c_size_t, i64, p]
+        f.restype = ctypes.c_int
     lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
     lib.cbc_read_status.restype = ctypes.c_int
     lib.cbc_profile_enable.argtypes = [i32]

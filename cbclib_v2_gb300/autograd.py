@@ -1,0 +1,146 @@
+"""Differentiable draw_lines: gradients of the drawn frames with respect to the line
+parameters (x0, y0, x1, y1, width), from the hand-written adjoint kernels
+(cbc_draw_lines_backward_*, csrc/cbc_adjoint.cu).
+
+``draw_lines_fn(lines, idxs, shape=..., max_val=..., kernel=..., overlap=...)`` returns
+new frames ``out0 + draw(lines)`` (``out0`` zeros unless given) and is differentiable
+with respect to ``lines`` and ``out0``.  For max overlap the gradient of a pixel goes
+to the line whose value the pixel kept (the first in line order among equal values),
+or to ``out0`` where no line raised the pixel.
+"""
+import math
+import threading
+from typing import Optional, Sequence
+
+import torch
+
+from . import _native, ndimage
+
+__all__ = ['draw_lines_fn', 'DrawLinesFunction', 'lines_backward']
+
+_ws_lock = threading.Lock()
+_workspaces = {}
+
+
+def _workspace(dev: torch.device, stream) -> ndimage.Workspace:
+    key = ('adjoint', dev.index, stream.cuda_stream, threading.get_ident())
+    with _ws_lock:
+        ws = _workspaces.get(key)
+        if ws is None:
+            ws = _workspaces[key] = ndimage.Workspace(dev)
+        return ws
+
+
+def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[torch.Tensor],
+                   max_val: float, kernel: str, overlap: str,
+                   image: Optional[torch.Tensor] = None, out0: Optional[torch.Tensor] = None,
+                   winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """(N, 5) gradient of sum(grad_out * draw_lines(...)) with respect to ``lines``.
+
+    ``grad_out`` has the frames' shape and dtype.  Max overlap also needs the forward
+    result ``image`` (and ``out0`` if the frames were not zeros); ``winner`` (int32,
+    frames' shape) is filled with each pixel's winning line when given."""
+    k, ov = ndimage._check_names(kernel, overlap)
+    dev, dtype = grad_out.device, grad_out.dtype
+    if dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"grad_out must be float32 or float64, got {dtype}")
+    ln = ndimage._as_device_lines(lines, dev, dtype)
+    n = ln.shape[0]
+    ix = ndimage._as_device_idxs(idxs, n, dev)
+    H, W = int(grad_out.shape[-2]), int(grad_out.shape[-1])
+    F = math.prod(int(s) for s in grad_out.shape[:-2])
+    g = grad_out.contiguous()
+    img = o0 = None
+    if ov == _native.OVERLAPS['max']:
+        if image is None:
+            raise ValueError("max overlap needs the forward image")
+        img = image.to(dtype).contiguous()
+        o0 = None if out0 is None else out0.to(dtype).contiguous()
+        if winner is None:
+            winner = torch.empty(grad_out.shape, dtype=torch.int32, device=dev)
+    grad = torch.empty((n, 5), dtype=dtype, device=dev)
+    lib = _native.lib()
+    elem = 4 if dtype == torch.float32 else 8
+    fn = lib.cbc_draw_lines_backward_f32 if elem == 4 else lib.cbc_draw_lines_backward_f64
+    with torch.cuda.device(dev):
+        stream = torch.cuda.current_stream(dev)
+        ws = _workspace(dev, stream)
+        ck_capacity = max(ws.ck_capacity, 16 * n + 1024)
+        for _ in range(4):
+            nbytes = lib.cbc_draw_lines_backward_workspace_size(n, ck_capacity, elem)
+            buf = ws.ensure(nbytes)
+            rc = fn(g.data_ptr(), F, H, W, ln.data_ptr(), n,
+                    None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                    max_val, k, ov, None if img is None else img.data_ptr(),
+                    None if o0 is None else o0.data_ptr(),
+                    None if winner is None else winner.data_ptr(), grad.data_ptr(),
+                    buf.data_ptr(), buf.numel(), ck_capacity, stream.cuda_stream)
+            if rc:
+                ndimage._raise_rc(rc)
+            st = _native.Status()
+            if lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream):
+                ndimage._raise_rc(_native.CBC_ERR_CUDA)
+            ndimage._raise_status(st, F)
+            if not st.has(_native.CBC_ERR_CAPACITY):
+                ws.ck_capacity = ck_capacity
+                return grad
+            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
+    raise RuntimeError("checkpoint capacity did not converge")
+
+
+class DrawLinesFunction(torch.autograd.Function):
+    """frames = out0 + draw_lines(lines); gradients for lines and out0."""
+
+    @staticmethod
+    def forward(ctx, lines, out0, idxs, max_val, kernel, overlap):
+        image = out0.detach().clone(memory_format=torch.contiguous_format)
+        k, ov = ndimage._check_names(kernel, overlap)
+        ndimage._draw_lines_cuda(image, lines.detach(), idxs, max_val, k, ov)
+        ctx.meta = (max_val, kernel, overlap)
+        if overlap == 'max':
+            ctx.save_for_backward(lines.detach(), idxs, image, out0.detach())
+        else:
+            ctx.save_for_backward(lines.detach(), idxs)
+        return image
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        max_val, kernel, overlap = ctx.meta
+        saved = ctx.saved_tensors
+        lines, idxs = saved[0], saved[1]
+        grad_lines = grad_out0 = None
+        g = grad_image.contiguous()
+        if overlap == 'max':
+            image, out0 = saved[2], saved[3]
+            winner = torch.empty(g.shape, dtype=torch.int32, device=g.device)
+            if ctx.needs_input_grad[0]:
+                grad_lines = lines_backward(g, lines, idxs, max_val, kernel, overlap, image,
+                                            out0, winner)
+            if ctx.needs_input_grad[1]:
+                if not ctx.needs_input_grad[0]:
+                    lines_backward(g, lines, idxs, max_val, kernel, overlap, image, out0, winner)
+                grad_out0 = torch.where(winner == _native.NO_WINNER, g, torch.zeros_like(g))
+        else:
+            if ctx.needs_input_grad[0]:
+                grad_lines = lines_backward(g, lines, idxs, max_val, kernel, overlap)
+            if ctx.needs_input_grad[1]:
+                grad_out0 = g
+        if grad_lines is not None:
+            grad_lines = grad_lines.to(lines.dtype).reshape(lines.shape)
+        return grad_lines, grad_out0, None, None, None, None
+
+
+def draw_lines_fn(lines: torch.Tensor, idxs: Optional[torch.Tensor] = None, *,
+                  shape: Optional[Sequence[int]] = None, out0: Optional[torch.Tensor] = None,
+                  max_val: float = 1.0, kernel: str = 'rectangular',
+                  overlap: str = 'sum') -> torch.Tensor:
+    """New frames ``out0 + draw_lines(lines)``, differentiable in ``lines`` (N, 5) and
+    ``out0``.  Give either ``shape`` (frames start at zero) or ``out0``."""
+    if out0 is None:
+        if shape is None:
+            raise ValueError("give shape or out0")
+        out0 = torch.zeros(tuple(shape), dtype=lines.dtype, device=lines.device)
+    if lines.shape[-1] != 5:
+        raise RuntimeError(f"Invalid lines size ({lines.shape[-1]}) at axis {lines.ndim - 1}")
+    ndimage._check_names(kernel, overlap)
+    return DrawLinesFunction.apply(lines, out0, idxs, float(max_val), kernel, overlap)

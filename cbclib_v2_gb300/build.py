@@ -11,8 +11,8 @@ CSRC = os.path.join(PKG, 'csrc')
 INCLUDE = os.path.join(ROOT, 'include')
 LIBDIR = os.path.join(PKG, '_lib')
 LIB = os.path.join(LIBDIR, 'libcbc_gb300.so')
-SOURCES = ['cbc_draw_lines.cu']
-DEPS = ['exact.cuh', 'exp_table.inc']
+SOURCES = ['cbc_draw_lines.cu', 'cbc_adjoint.cu']
+DEPS = ['exact.cuh', 'exp_table.inc', 'cbc_common.cuh']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 
@@ -38,13 +38,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)
     tmp = LIB + '.tmp'
-    cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', '--fmad=false',
-           '-Xcompiler', '-fPIC,-fvisibility=hidden', '-shared',
-           '-I', INCLUDE, '-I', CSRC, '-o', tmp]
+    flags = [*ARCH, '-O3', '-lineinfo', '-std=c++17', '--fmad=false',
+             '-Xcompiler', '-fPIC,-fvisibility=hidden', '-I', INCLUDE, '-I', CSRC]
     if verbose:
-        cmd += ['-Xptxas', '-v']
-    cmd += [os.path.join(CSRC, f) for f in SOURCES]
-    subprocess.run(cmd, check=True)
+        flags += ['-Xptxas', '-v']
+    objs = []
+    procs = []
+    for f in SOURCES:                       # translation units compile in parallel
+        obj = os.path.join(LIBDIR, os.path.splitext(f)[0] + '.o')
+        objs.append(obj)
+        procs.append(subprocess.Popen([nvcc(), *flags, '-c', os.path.join(CSRC, f), '-o', obj]))
+    if any(p.wait() != 0 for p in procs):
+        raise RuntimeError('nvcc failed')
+    subprocess.run([nvcc(), *ARCH, '-shared', '-o', tmp, *objs], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -1,0 +1,326 @@
+/*
+ * cbc_adjoint.cu — gradient of draw_lines with respect to the line parameters (no
+ * counterpart in the reference, which differentiates only its geometry).
+ *
+ * A line draws v = max_val * K(x), x = d / w, at every pixel its walk draws, d being
+ * the distance from the pixel to the segment (the walk's error E is (d / w)^2 in exact
+ * arithmetic, bresenham.hpp:291-296).  With q = p0 + s (p1 - p0) the nearest point of
+ * the segment (s clamped to [0, 1]) the envelope theorem gives
+ *     dv/dp0 = kappa (1 - s) (q - p),  dv/dp1 = kappa s (q - p),  dv/dw = -kappa d^2 / w
+ * with kappa = max_val K'(x) / (d w), which is finite at d = 0 for the smooth profiles
+ * (biweight -3.75 (1 - x^2) / w^2, gaussian -9 K(x) / w^2, parabolic -1.5 / w^2;
+ * rectangular 0; triangular -1 / (d w), taken as 0 at d = 0).
+ *
+ * The pixels are exactly the forward's: drive_segments (cbc_common.cuh) enumerates the
+ * walk with the reference's arithmetic.  For max overlap a first pass records, per
+ * pixel, the smallest line index whose exact value equals the final pixel value (and
+ * exceeds the value before drawing): sequential std::max keeps the first such line,
+ * so only that line receives the pixel's gradient.  Per-line sums are accumulated per
+ * segment in shared memory, then in double in global memory.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <limits.h>
+#include <string>
+
+#include "cbc_common.cuh"
+
+namespace cbc {
+
+
+/* max overlap: winner[p] = min over lines l with v_l(p) == image[p] > out0[p] */
+template <typename T, int K>
+struct WinnerAct {
+    const T *image;
+    const T *out0;       /* NULL: zeros */
+    int *winner;
+    T max_val;
+    int W;
+    __device__ __forceinline__ void item_begin(int) {}
+    __device__ __forceinline__ void item_end(int, const SlotLine<T> &) {}
+    __device__ __forceinline__ void pixel(const SlotParams<T> &, const SlotLine<T> &sl, int,
+                                          int px, int py, T E, T, T) {
+        using A = Ar<T>;
+        const long long at = sl.fbase + (long long)py * W + px;
+        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
+        const T img = image[at];
+        const T o = out0 ? out0[at] : T(0);
+        if (v == img && o < img) atomicMin(winner + at, sl.line);
+    }
+};
+
+template <typename T, int K>
+__device__ __forceinline__ T kappa_of(T d, T w, T max_val)
+{
+    const T x = d / w, ww = w * w;
+    switch (K) {
+    case CBC_BIWEIGHT:  return max_val * T(-3.75) * (T(1) - x * x) / ww;
+    case CBC_GAUSSIAN:  return max_val * T(-9) * T(CBC_GAUSS_C) * exp(T(-4.5) * x * x) / ww;
+    case CBC_PARABOLIC: return max_val * T(-1.5) / ww;
+    case CBC_RECTANGULAR: return T(0);
+    default:            return d > T(0) ? -max_val / (d * w) : T(0);
+    }
+}
+
+template <typename T, int K, int OV>
+struct BackwardAct {
+    const T *grad_out;
+    const int *winner;   /* max overlap */
+    double *gacc;        /* (N, 5) */
+    T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
+    T max_val;
+    int W;
+    __device__ __forceinline__ void item_begin(int lane) {
+        #pragma unroll
+        for (int k = 0; k < 5; k++) acc[lane][k] = T(0);
+    }
+    __device__ __forceinline__ void item_end(int lane, const SlotLine<T> &sl) {
+        if (sl.line < 0) return;
+        #pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const T v = acc[lane][k];
+            if (v != T(0)) atomicAdd(gacc + (size_t)sl.line * 5 + k, (double)v);
+        }
+    }
+    __device__ __forceinline__ void pixel(const SlotParams<T> &, const SlotLine<T> &sl, int slot,
+                                          int px, int py, T, T, T) {
+        const long long at = sl.fbase + (long long)py * W + px;
+        if (OV == CBC_MAX && winner[at] != sl.line) return;
+        const T g = grad_out[at];
+        if (g == T(0)) return;
+        const T X = (T)px, Y = (T)py;
+        const T cx = sl.x0 + T(0.5) * sl.t0, cy = sl.y0 + T(0.5) * sl.t1;
+        const T mag = sl.t0 * sl.t0 + sl.t1 * sl.t1;
+        T t = ((X - cx) * sl.t0 + (Y - cy) * sl.t1) / mag;
+        t = t < T(-0.5) ? T(-0.5) : (t > T(0.5) ? T(0.5) : t);
+        const T dx = cx + t * sl.t0 - X, dy = cy + t * sl.t1 - Y;
+        const T d2 = dx * dx + dy * dy;
+        const T d = sqrt(d2);
+        const T G = g * kappa_of<T, K>(d, sl.w, max_val);
+        if (G == T(0)) return;
+        const T s = t + T(0.5);
+        atomicAdd(&acc[slot][0], G * (T(1) - s) * dx);
+        atomicAdd(&acc[slot][1], G * (T(1) - s) * dy);
+        atomicAdd(&acc[slot][2], G * s * dx);
+        atomicAdd(&acc[slot][3], G * s * dy);
+        atomicAdd(&acc[slot][4], -G * d2 / sl.w);
+    }
+};
+
+template <typename T>
+struct AdjArgs {
+    DriveArgs<T> d;
+    const T *grad_out;
+    const T *image;
+    const T *out0;
+    int *winner;
+    double *gacc;
+    T max_val;
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kSegWarps * 32)
+winner_kernel(AdjArgs<T> a)
+{
+    WinnerAct<T, K> act;
+    act.image = a.image;
+    act.out0 = a.out0;
+    act.winner = a.winner;
+    act.max_val = a.max_val;
+    act.W = a.d.W;
+    drive_segments(a.d, act);
+}
+
+template <typename T, int K, int OV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+backward_kernel(AdjArgs<T> a)
+{
+    __shared__ T acc_s[kSegWarps][32][5];
+    BackwardAct<T, K, OV> act;
+    act.grad_out = a.grad_out;
+    act.winner = a.winner;
+    act.gacc = a.gacc;
+    act.acc = acc_s[threadIdx.x >> 5];
+    act.max_val = a.max_val;
+    act.W = a.d.W;
+    drive_segments(a.d, act);
+}
+
+template <typename T>
+__global__ void finalize_kernel(const double *gacc, T *grad_lines, long long n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) grad_lines[i] = (T)gacc[i];
+}
+
+struct AdjLayout {
+    size_t status, recs, cks, gacc, total;
+};
+
+AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes, size_t ck_bytes)
+{
+    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+    AdjLayout L;
+    size_t off = 0;
+    L.status = off; off = up(off + sizeof(DevStatus));
+    L.recs = off;   off = up(off + rec_bytes * (size_t)n_lines);
+    L.cks = off;    off = up(off + ck_bytes * (size_t)ck_capacity);
+    L.gacc = off;   off = up(off + sizeof(double) * 5 * (size_t)n_lines);
+    L.total = off;
+    return L;
+}
+
+template <typename T, int K>
+cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, int grid, cudaStream_t s)
+{
+    if (overlap == CBC_MAX) {
+        winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return e;
+        backward_kernel<T, K, CBC_MAX><<<grid, kSegWarps * 32, 0, s>>>(aa);
+    } else {
+        backward_kernel<T, K, CBC_SUM><<<grid, kSegWarps * 32, 0, s>>>(aa);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+int backward_impl(const T *grad_out, long long n_frames, long long H, long long W,
+                  const T *lines, long long n_lines, const void *idxs, int idx_bytes,
+                  T max_val, int kernel, int overlap, const T *image, const T *out0,
+                  int *winner, T *grad_lines, void *workspace, size_t ws_bytes,
+                  long long ck_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (H > INT_MAX / 2 || W > INT_MAX / 2)
+        return fail(CBC_ERR_INVALID, "frame dimensions must be below 2^30");
+    if (kernel < 0 || kernel > 4) return fail(CBC_ERR_INVALID, "Invalid kernel type");
+    if (overlap != CBC_SUM && overlap != CBC_MAX)
+        return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if (idxs && idx_bytes != 4 && idx_bytes != 8)
+        return fail(CBC_ERR_INVALID, "idx_bytes must be 4 or 8");
+    if (!idxs && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
+        return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
+                                         " != " + std::to_string(n_frames) + ")");
+    if (n_lines > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
+    const bool pixels = n_frames * H * W > 0;
+    if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_lines > 0 && pixels && !grad_out) return fail(CBC_ERR_INVALID, "null grad_out");
+    if (overlap == CBC_MAX && n_lines > 0 && pixels && (!image || !winner))
+        return fail(CBC_ERR_INVALID, "max overlap needs the forward image and a winner buffer");
+    AdjLayout L = adj_layout(n_lines, ck_capacity, sizeof(LineRec<T>), sizeof(Checkpoint<T>));
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
+    Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
+    double *gacc = reinterpret_cast<double *>(ws + L.gacc);
+    init_status_kernel<<<1, 1, 0, s>>>(st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines == 0) return CBC_OK;
+    e = cudaMemsetAsync(gacc, 0, sizeof(double) * 5 * (size_t)n_lines, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    Geometry g;
+    g.H = (int)H;
+    g.W = (int)W;
+    g.tile_w = g.tile_h = 64;
+    g.tiles_x = g.tiles_y = 1;
+    const unsigned nb = (unsigned)((n_lines + 255) / 256);
+    if (idxs && idx_bytes == 8)
+        prep_kernel<T, int64_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
+                                                                recs, nullptr, cks, ck_capacity, st);
+    else
+        prep_kernel<T, int32_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
+                                                                recs, nullptr, cks, ck_capacity, st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (pixels) {
+        if (overlap == CBC_MAX) {
+            e = cudaMemsetAsync(winner, 0x7f, sizeof(int) * (size_t)(n_frames * H * W), s);
+            if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        }
+        AdjArgs<T> aa;
+        aa.d.recs = recs;
+        aa.d.cks = cks;
+        aa.d.H = (int)H;
+        aa.d.W = (int)W;
+        aa.d.st = st;
+        aa.d.work = &st->work;
+        aa.grad_out = grad_out;
+        aa.image = image;
+        aa.out0 = out0;
+        aa.winner = winner;
+        aa.gacc = gacc;
+        aa.max_val = max_val;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = sms > 0 ? sms * 8 : 1024;
+        switch (kernel) {
+        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, grid, s); break;
+        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, grid, s); break;
+        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, grid, s); break;
+        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, grid, s); break;
+        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, grid, s); break;
+        }
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const long long n5 = 5 * n_lines;
+    finalize_kernel<T><<<(unsigned)((n5 + 255) / 256), 256, 0, s>>>(gacc, grad_lines, n5);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
+}  // namespace cbc
+
+extern "C" {
+
+size_t cbc_draw_lines_backward_workspace_size(int64_t n_lines, int64_t checkpoint_capacity,
+                                              int32_t elem_bytes)
+{
+    if (n_lines < 0 || checkpoint_capacity < 0) return 0;
+    size_t rec = elem_bytes == 8 ? sizeof(cbc::LineRec<double>) : sizeof(cbc::LineRec<float>);
+    size_t ck = elem_bytes == 8 ? sizeof(cbc::Checkpoint<double>) : sizeof(cbc::Checkpoint<float>);
+    return cbc::adj_layout(n_lines, checkpoint_capacity, rec, ck).total;
+}
+
+int cbc_draw_lines_backward_f32(const float *grad_out, int64_t n_frames, int64_t height,
+                                int64_t width, const float *lines, int64_t n_lines,
+                                const void *idxs, int32_t idx_bytes, float max_val,
+                                int32_t kernel, int32_t overlap, const float *image,
+                                const float *out0, int32_t *winner, float *grad_lines,
+                                void *workspace, size_t workspace_bytes,
+                                int64_t checkpoint_capacity, void *stream)
+{
+    return cbc::backward_impl<float>(grad_out, n_frames, height, width, lines, n_lines, idxs,
+                                     idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                     grad_lines, workspace, workspace_bytes, checkpoint_capacity,
+                                     stream);
+}
+
+int cbc_draw_lines_backward_f64(const double *grad_out, int64_t n_frames, int64_t height,
+                                int64_t width, const double *lines, int64_t n_lines,
+                                const void *idxs, int32_t idx_bytes, double max_val,
+                                int32_t kernel, int32_t overlap, const double *image,
+                                const double *out0, int32_t *winner, double *grad_lines,
+                                void *workspace, size_t workspace_bytes,
+                                int64_t checkpoint_capacity, void *stream)
+{
+    return cbc::backward_impl<double>(grad_out, n_frames, height, width, lines, n_lines, idxs,
+                                      idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                      grad_lines, workspace, workspace_bytes,
+                                      checkpoint_capacity, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,859 @@
+/*
+ * cbc_common.cuh — device code shared by the forward (cbc_draw_lines.cu) and the
+ * adjoint (cbc_adjoint.cu): per-line records, the reference's walk in exact float
+ * arithmetic, tile coverage, walk checkpoints and the span helpers.
+ */
+#ifndef CBC_COMMON_CUH
+#define CBC_COMMON_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <limits.h>
+#include <string>
+
+#include "cbc_draw_lines.h"
+#include "exact.cuh"
+
+namespace cbc {
+
+constexpr int kThreads = 256;
+constexpr int kMaxChunk = 32;
+constexpr int kDefaultTileW = 64;
+constexpr int kDefaultTileH = 64;
+constexpr int kDefaultChunk = 16;
+constexpr int kFatal = (1 << CBC_ERR_INDEX) | (1 << CBC_ERR_CAPACITY) | (1 << CBC_ERR_RANGE);
+constexpr int kInvalidEntry = INT_MIN;
+
+/* ---- per-line walk record ------------------------------------------------------ */
+
+enum : int { kAxisY = 1, kStepXNeg = 2, kStepYNeg = 4, kDrawable = 8, kFastDiv = 16 };
+
+/* BresenhamPlotter state of one 2-D line (bresenham.hpp:243-263): the walk starts at
+ * (x0, y0) = m_pt0 and ends when a coordinate reaches (x1, y1) = m_pt1 (step added). */
+template <typename T>
+struct alignas(16) LineRec {
+    int32_t x0, y0, x1, y1;
+    T t0, t1;        /* tangent pt1 - pt0; the normal is (t1, -t0)             */
+    T len, len2;     /* amplitude(tangent), len * len                          */
+    T w, ww;         /* width, width * width                                   */
+    T te0, ne0;      /* tangent / normal errors at the walk start              */
+    T px, py;        /* pt0, for the tile coverage only                        */
+    T rlen, rww;     /* RN(1 / len), RN(1 / ww) for the division shortcut      */
+    T ne_thr;        /* spans continue while |ne| < ne_thr (see span_threshold) */
+    int32_t frame, flags;
+    int32_t c0;      /* first in-frame long coordinate of the walk, in walk order  */
+    int32_t ncols;   /* in-frame long coordinates of the walk                      */
+    int32_t ck_base; /* index of the line's first walk checkpoint                  */
+    int32_t pad;
+};
+
+/* the walk's exact iterator state at the first position whose walk index
+ * (c - c0) * step_long reaches a multiple of kSeg (cx = INT_MIN: the walk ends first) */
+constexpr int kSeg = 8;
+
+template <typename T>
+struct Checkpoint {
+    int32_t cx, cy;
+    T te, ne;
+    int32_t line;   /* owning line                  */
+    int32_t seg;    /* segment index within the line */
+};
+
+/* status block at the start of the workspace */
+struct DevStatus {
+    int flags;
+    int reserved;
+    unsigned long long bad_line;
+    long long idx_min;
+    long long idx_max;
+    unsigned long long pairs;      /* running pair cursor == pairs_needed */
+    unsigned long long cks;        /* running checkpoint cursor            */
+    unsigned long long work;       /* work-item counter of the lines render */
+};
+
+/* per line of the current render chunk */
+template <typename T>
+struct SlotParams {
+    T ts, ns;           /* tangent / normal derivative along the short axis           */
+    T len, len2, ww;
+    T rlen, rww;
+    T ne_thr;           /* span continuation threshold on |ne|                         */
+    float rns;          /* ~1 / ns, for the span window estimate only                 */
+    int ss;             /* step sign along the short axis (first span half)            */
+    int axis;
+    int fast;           /* len and ww in the range of the division shortcut            */
+};
+
+/* per line of the current render chunk: what the segment replays need */
+template <typename T>
+struct WalkSlot {
+    T d0t, d1t, d0n, d1n;   /* step * tangent, step * normal per axis     */
+    int sx, sy;
+    int x1, y1;             /* walk end                                   */
+    int c0, sa;             /* walk index = (c - c0) * sa                 */
+    int k_lo, k_hi;         /* walk indices of the in-tile columns        */
+    int ck_base;
+    int ent_base;           /* entry pool index of walk index k_lo        */
+    int seg_base;           /* first flattened segment item of this line  */
+    int axis;
+};
+
+/* ---- arithmetic in the reference's rounding ----------------------------------- */
+
+template <typename T> struct Ar;
+
+template <> struct Ar<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
+    static __device__ __forceinline__ float from_int(int v) { return __int2float_rn(v); }
+    static __device__ __forceinline__ float nterm(float ne, const SlotParams<float> &p) {
+        return p.fast ? cbc_normal_term_r(ne, p.len, p.rlen) : cbc_normal_term(ne, p.len);
+    }
+    static __device__ __forceinline__ float error(float te, float nf, const SlotParams<float> &p) {
+        return p.fast ? cbc_pixel_error_r(te, nf, p.len, p.len2, p.ww, p.rlen, p.rww)
+                      : cbc_pixel_error(te, nf, p.len, p.len2, p.ww);
+    }
+    template <int K>
+    static __device__ __forceinline__ float profile(float x) { return cbc_profile_f32(K, x); }
+    static __device__ __forceinline__ bool fast_range(float v) {
+        return v >= CBC_DIV_LO && v <= CBC_DIV_HI;
+    }
+};
+
+template <> struct Ar<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double sqrt(double a) { return __dsqrt_rn(a); }
+    static __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
+    static __device__ __forceinline__ double from_int(int v) { return (double)v; }
+    /* normal_error: T accumulator fed with pow(b, 2) = fl(b * b) (bresenham.hpp:284-289) */
+    static __device__ __forceinline__ double nterm(double ne, const SlotParams<double> &p) {
+        double b = __ddiv_rn(ne, p.len);
+        return __dmul_rn(b, b);
+    }
+    /* error(): fl(fl(fl(a * a) + nf) / ww) (bresenham.hpp:291-296) */
+    static __device__ __forceinline__ double error(double te, double nf,
+                                                   const SlotParams<double> &p) {
+        double m1 = -te, m2 = __dsub_rn(te, p.len2);
+        double ta = (m1 < m2) ? m2 : m1;
+        if (ta < 0.0) ta = 0.0;
+        double a = __ddiv_rn(ta, p.len);
+        return __ddiv_rn(__dadd_rn(__dmul_rn(a, a), nf), p.ww);
+    }
+    template <int K>
+    static __device__ __forceinline__ double profile(double x) { return cbc_profile_f64(K, x); }
+    static __device__ __forceinline__ bool fast_range(double) { return false; }
+};
+
+/* ---- line preparation ---------------------------------------------------------- */
+
+template <typename T>
+__device__ __forceinline__ bool finite_val(T v) { return isfinite(v); }
+
+/* The span loops of draw_line_2d continue while normal_error < width^2, with
+ * normal_error = fl(fl(ne / len)^2) (bresenham.hpp:369-380).  That is a monotone
+ * function of |ne| (round-to-nearest is monotone and odd), so the test equals
+ * |ne| < ne_thr for ne_thr = the least non-negative float with
+ * fl(fl(ne_thr / len)^2) >= ww, found by bisection over the float bit patterns. */
+template <typename T>
+__device__ T span_threshold(T len, T ww);
+
+template <>
+__device__ inline float span_threshold<float>(float len, float ww)
+{
+    unsigned lo = 0u, hi = 0x7f800000u;              /* f(+inf) = inf >= ww */
+    while (lo < hi) {
+        unsigned mid = lo + ((hi - lo) >> 1);
+        float b = __fdiv_rn(__uint_as_float(mid), len);
+        if (__fmul_rn(b, b) >= ww) hi = mid; else lo = mid + 1;
+    }
+    return __uint_as_float(lo);
+}
+
+template <>
+__device__ inline double span_threshold<double>(double len, double ww)
+{
+    unsigned long long lo = 0ull, hi = 0x7ff0000000000000ull;
+    while (lo < hi) {
+        unsigned long long mid = lo + ((hi - lo) >> 1);
+        double b = __ddiv_rn(__longlong_as_double((long long)mid), len);
+        if (__dmul_rn(b, b) >= ww) hi = mid; else lo = mid + 1;
+    }
+    return __longlong_as_double((long long)lo);
+}
+
+/* BresenhamPlotter(line, long(ceil(width) + 1)) (bresenham.hpp:243-253) plus begin()
+ * (:255-263).  Returns false for lines that draw nothing in the reference (zero
+ * length, non-positive width) or whose walk is not defined (non-finite values). */
+template <typename T>
+__device__ bool build_rec(const T *ln, LineRec<T> &r, bool &too_long)
+{
+    using A = Ar<T>;
+    too_long = false;
+    T p0x = ln[0], p0y = ln[1], p1x = ln[2], p1y = ln[3], w = ln[4];
+    if (!(finite_val(p0x) && finite_val(p0y) && finite_val(p1x) && finite_val(p1y) &&
+          finite_val(w)))
+        return false;
+    if (!(w > T(0))) return false;            /* error() is +inf for width <= 0 */
+    T t0 = A::sub(p1x, p0x), t1 = A::sub(p1y, p0y);
+    int axis = (fabs(t0) < fabs(t1)) ? 1 : 0; /* first max |tau| */
+    T mag = A::add(A::mul(t0, t0), A::mul(t1, t1));
+    T len = A::sqrt(mag);
+    if (!(len > T(0))) return false;          /* error() is NaN everywhere */
+    T ceilw = A::add(ceil(w), T(1));
+    if (!(ceilw < T(1e9))) return false;
+    T tn0 = A::div(t0, len), tn1 = A::div(t1, len);
+    T scale = fabs(A::div(ceilw, axis ? tn1 : tn0));
+    int sx = (p1x >= p0x) ? 1 : -1, sy = (p1y >= p0y) ? 1 : -1;
+    T a0 = round(A::sub(p0x, A::mul(scale, tn0)));
+    T a1 = round(A::sub(p0y, A::mul(scale, tn1)));
+    T b0 = round(A::add(p1x, A::mul(scale, tn0)));
+    T b1 = round(A::add(p1y, A::mul(scale, tn1)));
+    const T lim = T(1 << 30);
+    if (!(fabs(a0) < lim && fabs(a1) < lim && fabs(b0) < lim && fabs(b1) < lim)) {
+        too_long = true;
+        return false;
+    }
+    r.x0 = (int32_t)a0;
+    r.y0 = (int32_t)a1;
+    r.x1 = (int32_t)b0 + sx;
+    r.y1 = (int32_t)b1 + sy;
+    long long walk = axis ? (long long)r.y1 - r.y0 : (long long)r.x1 - r.x0;
+    if (walk < 0) walk = -walk;
+    /* spans reach width * len / |t_long| pixels off the line along the short axis */
+    T span = A::div(A::mul(w, len), fabs(axis ? t1 : t0));
+    if (walk > CBC_MAX_WALK || !(span < T(CBC_MAX_WALK))) {
+        too_long = true;
+        return false;
+    }
+    T d0 = A::sub(A::from_int(r.x0), p0x), d1 = A::sub(A::from_int(r.y0), p0y);
+    r.t0 = t0;
+    r.t1 = t1;
+    r.len = len;
+    r.len2 = A::mul(len, len);
+    r.w = w;
+    r.ww = A::mul(w, w);
+    r.te0 = A::add(A::mul(t0, d0), A::mul(t1, d1));
+    r.ne0 = A::add(A::mul(t1, d0), A::mul(-t0, d1));
+    r.px = p0x;
+    r.py = p0y;
+    r.rlen = A::rcp(len);
+    r.rww = A::rcp(r.ww);
+    bool fast = A::fast_range(len) && A::fast_range(r.ww);
+    r.ne_thr = span_threshold<T>(len, r.ww);
+    r.flags = axis | (sx < 0 ? kStepXNeg : 0) | (sy < 0 ? kStepYNeg : 0) | kDrawable |
+              (fast ? kFastDiv : 0);
+    return true;
+}
+
+struct Geometry {
+    int H, W;
+    int tile_w, tile_h;
+    int tiles_x, tiles_y;
+};
+
+/* Conservative tile coverage of the pixels the walk can draw.  The walk covers the
+ * long-axis range [m_pt0, m_pt1) exactly; at long coordinate c its centre pixel lies
+ * within 1 px of the line and its spans stop where |normal distance| >= width, i.e.
+ * within width * len / |t_long| of the line along the short axis. */
+template <typename T>
+struct Coverage {
+    int a, sa;          /* long axis, walk direction along it                          */
+    int lmin, lmax;     /* long-axis range of the walk inside the frame                */
+    int TA, TS;         /* tile extents along the long / short axis                    */
+    int ext_s;
+    float ps, pa, slope, hw;
+
+    __device__ bool init(const LineRec<T> &r, const Geometry &g) {
+        a = r.flags & kAxisY;
+        const int sxs = (r.flags & kStepXNeg) ? -1 : 1, sys = (r.flags & kStepYNeg) ? -1 : 1;
+        sa = a ? sys : sxs;
+        int first = a ? r.y0 : r.x0;
+        int last = (a ? r.y1 : r.x1) - sa;
+        lmin = max(min(first, last), 0);
+        const int ext_a = a ? g.H : g.W;
+        ext_s = a ? g.W : g.H;
+        lmax = min(max(first, last), ext_a - 1);
+        TA = a ? g.tile_h : g.tile_w;
+        TS = a ? g.tile_w : g.tile_h;
+        const float ta = (float)(a ? r.t1 : r.t0), ts = (float)(a ? r.t0 : r.t1);
+        pa = (float)(a ? r.py : r.px);
+        ps = (float)(a ? r.px : r.py);
+        slope = ts / ta;
+        hw = (float)r.w * (float)r.len / fabsf(ta) + 2.0f;
+        return lmin <= lmax;
+    }
+    /* tile rows (short-axis tile indices) [j0, j1] of tile column ti; false if none */
+    __device__ bool rows(int ti, int &j0, int &j1) const {
+        int ca = max(lmin, ti * TA), cb = min(lmax, ti * TA + TA - 1);
+        float s0 = ps + ((float)ca - pa) * slope, s1 = ps + ((float)cb - pa) * slope;
+        float smin = fminf(s0, s1) - hw, smax = fmaxf(s0, s1) + hw;
+        if (!(smax >= 0.0f) || !(smin <= (float)(ext_s - 1))) return false;
+        j0 = max(0, (int)floorf(fmaxf(smin, -1.0f))) / TS;
+        j1 = min(ext_s - 1, (int)floorf(fminf(smax, (float)ext_s))) / TS;
+        return j0 <= j1;
+    }
+    __device__ int bin(int ti, int tj, const Geometry &g) const {
+        return a ? (ti * g.tiles_x + tj) : (tj * g.tiles_x + ti);
+    }
+};
+
+/* the reference's outer-walk step (LineIterator::update + operator++, bresenham.hpp:
+ * 205-220 and 98-111, for the single axis pair of 2-D) */
+template <typename T>
+struct Walker {
+    int cx, cy;
+    T te, ne;
+    int sx, sy;
+    T d0t, d1t, d0n, d1n;   /* step * tangent, step * normal per axis */
+
+    __device__ void init(const LineRec<T> &r) {
+        sx = (r.flags & kStepXNeg) ? -1 : 1;
+        sy = (r.flags & kStepYNeg) ? -1 : 1;
+        d0t = sx > 0 ? r.t0 : -r.t0;
+        d1t = sy > 0 ? r.t1 : -r.t1;
+        d0n = sx > 0 ? r.t1 : -r.t1;
+        d1n = sy > 0 ? -r.t0 : r.t0;
+    }
+    /* decisions at the current position: (next x, next y) */
+    __device__ __forceinline__ void decide(bool &nx, bool &ny, T &exx) const {
+        using A = Ar<T>;
+        exx = A::add(ne, d0n);
+        T eyy = A::add(ne, d1n);
+        T exy = A::add(exx, d1n);
+        if (fabs(eyy) < fabs(exx)) { ny = true; nx = fabs(exy) < fabs(eyy); }
+        else                       { nx = true; ny = fabs(exy) < fabs(exx); }
+    }
+    __device__ __forceinline__ void step(bool nx, bool ny, T exx) {
+        using A = Ar<T>;
+        if (nx) { cx += sx; te = A::add(te, d0t); ne = exx; }
+        if (ny) { cy += sy; te = A::add(te, d1t); ne = A::add(ne, d1n); }
+    }
+};
+
+template <typename IdxT>
+__device__ __forceinline__ long long load_idx(const void *idxs, long long i)
+{
+    return (long long)static_cast<const IdxT *>(idxs)[i];
+}
+
+/* warp-aggregated min / max of the frame indices, for the reference's error text */
+__device__ __forceinline__ void warp_minmax(long long v, bool valid, DevStatus *st)
+{
+    long long mn = valid ? v : LLONG_MAX, mx = valid ? v : LLONG_MIN;
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0 && mn <= mx) {
+        atomicMin(&st->idx_min, mn);
+        atomicMax(&st->idx_max, mx);
+    }
+}
+
+template <typename T>
+__device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> &cv,
+                                  Checkpoint<T> *__restrict__ cks, DevStatus *st);
+
+/* COUNT_TILES: count the line's (frame, tile) bins (tiles strategy); WALK: also write
+ * its walk checkpoints here (lines strategy, which needs no bins) */
+template <typename T, typename IdxT, bool COUNT_TILES, bool WALK>
+__global__ void __launch_bounds__(kThreads)
+prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
+            long long n_frames, Geometry g, LineRec<T> *__restrict__ recs,
+            int *__restrict__ counts, Checkpoint<T> *__restrict__ cks, long long ck_capacity,
+            DevStatus *st)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n_lines;
+    long long frame = 0;
+    const bool has_idx = idxs != nullptr;
+    if (in) frame = has_idx ? load_idx<IdxT>(idxs, i) : (n_frames == 1 ? 0 : i);
+    if (has_idx) warp_minmax(frame, in, st);
+    LineRec<T> r;
+    r.flags = 0;
+    int nck = 0;
+    Coverage<T> cv;
+    if (in) {
+        if (frame < 0 || frame >= n_frames) {
+            atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
+            atomicMin(&st->bad_line, (unsigned long long)i);
+        } else {
+            bool too_long = false;
+            if (build_rec(lines + 5 * i, r, too_long)) {
+                r.frame = (int32_t)frame;
+                if (cv.init(r, g)) {
+                    r.ncols = cv.lmax - cv.lmin + 1;
+                    r.c0 = cv.sa > 0 ? cv.lmin : cv.lmax;
+                    nck = (r.ncols + kSeg - 1) / kSeg;
+                } else {
+                    r.flags = 0;        /* walk never enters the frame */
+                }
+            } else {
+                r.flags = 0;
+                if (too_long) {
+                    atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+                    atomicMin(&st->bad_line, (unsigned long long)i);
+                }
+            }
+        }
+    }
+    /* checkpoint blocks: one atomic per warp on the checkpoint cursor */
+    const int lane = threadIdx.x & 31;
+    int incl = nck;
+    for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    unsigned long long wbase = 0;
+    if (lane == 31) wbase = atomicAdd(&st->cks, (unsigned long long)incl);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    if (!in) return;
+    if (r.flags & kDrawable) {
+        unsigned long long cb = wbase + (unsigned long long)(incl - nck);
+        const bool ck_ok = cb + (unsigned long long)nck <= (unsigned long long)ck_capacity;
+        if (!ck_ok) {
+            atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+            r.ck_base = 0;
+        } else {
+            r.ck_base = (int32_t)cb;
+        }
+        if (COUNT_TILES) {
+            int *fc = counts + (size_t)frame * g.tiles_x * g.tiles_y;
+            for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
+                int j0, j1;
+                if (!cv.rows(ti, j0, j1)) continue;
+                for (int tj = j0; tj <= j1; tj++) atomicAdd(fc + cv.bin(ti, tj, g), 1);
+            }
+        }
+        if (WALK && ck_ok) write_checkpoints(r, (int)i, cv, cks, st);
+    }
+    recs[i] = r;
+}
+
+static __global__ void init_status_kernel(DevStatus *st)
+{
+    st->flags = 0;
+    st->reserved = 0;
+    st->bad_line = ~0ull >> 1;
+    st->idx_min = LLONG_MAX;
+    st->idx_max = LLONG_MIN;
+    st->pairs = 0;
+    st->cks = 0;
+    st->work = 0;
+}
+
+/* bin offsets: block-local exclusive scan + one atomic per block on the pair cursor */
+static __global__ void __launch_bounds__(kThreads)
+offsets_kernel(const int *__restrict__ counts, int *__restrict__ offsets,
+               int *__restrict__ fillpos, long long n_bins, long long capacity, DevStatus *st)
+{
+    __shared__ int warp_sums[kThreads / 32];
+    __shared__ unsigned long long block_base;
+    long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = b < n_bins ? counts[b] : 0;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int v = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        int s = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += u;
+        }
+        if (lane < kThreads / 32) warp_sums[lane] = s - v;
+        if (lane == kThreads / 32 - 1) block_base = atomicAdd(&st->pairs, (unsigned long long)s);
+    }
+    __syncthreads();
+    if (b >= n_bins) return;
+    unsigned long long off = block_base + (unsigned long long)(warp_sums[wid] + incl - c);
+    if (c > 0 && off + (unsigned long long)c > (unsigned long long)capacity)
+        atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+    int o32 = off > (unsigned long long)INT_MAX ? INT_MAX : (int)off;
+    offsets[b] = o32;
+    fillpos[b] = o32;
+}
+
+/* walk line i once and store the iterator state every kSeg walk columns inside the
+ * frame (LineIterator state: position and both errors) */
+template <typename T>
+__device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> &cv,
+                                  Checkpoint<T> *__restrict__ cks, DevStatus *st)
+{
+    Walker<T> wk;
+    wk.init(r);
+    wk.cx = r.x0;
+    wk.cy = r.y0;
+    wk.te = r.te0;
+    wk.ne = r.ne0;
+    const int nck = (r.ncols + kSeg - 1) / kSeg;
+    Checkpoint<T> *ck = cks + r.ck_base;
+    int k = 0;
+    long long guard = 0;
+    while (k < nck && wk.cx != r.x1 && wk.cy != r.y1) {
+        const int idx = ((cv.a ? wk.cy : wk.cx) - r.c0) * cv.sa;
+        while (k < nck && idx >= k * kSeg) {
+            Checkpoint<T> c;
+            c.cx = wk.cx;
+            c.cy = wk.cy;
+            c.te = wk.te;
+            c.ne = wk.ne;
+            c.line = i;
+            c.seg = k;
+            ck[k++] = c;
+        }
+        bool nx, ny;
+        T exx;
+        wk.decide(nx, ny, exx);
+        wk.step(nx, ny, exx);
+        if (++guard > 4LL * CBC_MAX_WALK + 64) {
+            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+            break;
+        }
+    }
+    for (; k < nck; k++) {
+        Checkpoint<T> c;
+        c.cx = INT_MIN;
+        c.cy = 0;
+        c.te = T(0);
+        c.ne = T(0);
+        c.line = i;
+        c.seg = k;
+        ck[k] = c;
+    }
+}
+
+/* tiles strategy: one thread per line writes the line id into each of its bins and
+ * then its walk checkpoints */
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+fill_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
+            int *__restrict__ fillpos, int *__restrict__ pairs, long long capacity,
+            Checkpoint<T> *__restrict__ cks, DevStatus *st)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    if (st->flags & kFatal) return;
+    const LineRec<T> r = recs[i];
+    if (!(r.flags & kDrawable)) return;
+    Coverage<T> cv;
+    if (!cv.init(r, g)) return;
+    int *fp = fillpos + (size_t)r.frame * g.tiles_x * g.tiles_y;
+    for (int ti = cv.lmin / cv.TA; ti <= cv.lmax / cv.TA; ti++) {
+        int j0, j1;
+        if (!cv.rows(ti, j0, j1)) continue;
+        for (int tj = j0; tj <= j1; tj++) {
+            int pos = atomicAdd(fp + cv.bin(ti, tj, g), 1);
+            if (pos < capacity) pairs[pos] = (int)i;
+        }
+    }
+    write_checkpoints(r, (int)i, cv, cks, st);
+}
+
+/* lines strategy: one thread per line writes its walk checkpoints */
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+walk_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
+            Checkpoint<T> *__restrict__ cks, DevStatus *st)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    if (st->flags & kFatal) return;
+    const LineRec<T> r = recs[i];
+    if (!(r.flags & kDrawable)) return;
+    Coverage<T> cv;
+    if (!cv.init(r, g)) return;
+    write_checkpoints(r, (int)i, cv, cks, st);
+}
+
+/* ---- render ---------------------------------------------------------------------- */
+
+template <typename T>
+struct Entry {          /* one filled walk position (column) of a line inside the tile */
+    int c;              /* long-axis coordinate                                       */
+    int sc;             /* short-axis coordinate of the centre pixel                  */
+    T te, ne;           /* tangent / normal errors there                              */
+};
+
+template <typename T> struct Sentinel;
+/* sum: -0 is the only value that no contribution leaves behind (-0 + v = v, and
+ * -0 + +0 = +0); max: -inf, below every contribution that can change out */
+template <> struct Sentinel<float> {
+    static __device__ __forceinline__ float sum() { return -0.0f; }
+    static __device__ __forceinline__ bool sum_touched(float v) { return __float_as_uint(v) != 0x80000000u; }
+};
+template <> struct Sentinel<double> {
+    static __device__ __forceinline__ double sum() { return -0.0; }
+    static __device__ __forceinline__ bool sum_touched(double v) {
+        return (unsigned long long)__double_as_longlong(v) != 0x8000000000000000ull;
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ void combine_max(T *addr, T v);
+
+template <>
+__device__ __forceinline__ void combine_max<float>(float *addr, float v)
+{
+    /* acc = std::max(acc, v): replace only when acc < v (bresenham.cpp:71) */
+    unsigned *ua = reinterpret_cast<unsigned *>(addr);
+    unsigned old = *reinterpret_cast<volatile unsigned *>(ua);
+    while (__uint_as_float(old) < v) {
+        unsigned prev = atomicCAS(ua, old, __float_as_uint(v));
+        if (prev == old) break;
+        old = prev;
+    }
+}
+
+template <>
+__device__ __forceinline__ void combine_max<double>(double *addr, double v)
+{
+    unsigned long long *ua = reinterpret_cast<unsigned long long *>(addr);
+    unsigned long long old = *reinterpret_cast<volatile unsigned long long *>(ua);
+    while (__longlong_as_double((long long)old) < v) {
+        unsigned long long prev = atomicCAS(ua, old, (unsigned long long)__double_as_longlong(v));
+        if (prev == old) break;
+        old = prev;
+    }
+}
+
+/* window [jlo, jhi] of short-axis offsets from the centre that the span can reach:
+ * ne moves by ns per step, the span stops once |ne| >= ne_thr (float estimate, one
+ * pixel of margin each side), clipped to the frame / tile range [s_lo, s_hi] */
+template <typename T>
+__device__ __forceinline__ int span_window(const SlotParams<T> &p, int sc, T ne, int s_lo,
+                                           int s_hi, int &jlo)
+{
+    const float R = (float)p.ne_thr * fabsf(p.rns);
+    const float u = (float)ne * p.rns;
+    const float up = R - u, dn = R + u;
+    const int kp = up < 2e9f ? (int)floorf(up) + 1 : INT_MAX / 4;
+    const int km = dn < 2e9f ? (int)floorf(dn) + 1 : INT_MAX / 4;
+    jlo = max(-max(km, 0), s_lo - sc);
+    const int jhi = min(max(kp, 0), s_hi - sc);
+    return max(0, jhi - jlo + 1);
+}
+
+template <typename T>
+__device__ __forceinline__ void global_combine_max(T *addr, T v);
+
+template <>
+__device__ __forceinline__ void global_combine_max<float>(float *addr, float v)
+{
+    if (v > 0.0f) {
+        /* positive v: the integer order of the bit patterns is std::max's order for
+         * every out except a negative-signed NaN */
+        atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+    } else if (v == v) {
+        combine_max(addr, v);
+    }
+}
+
+template <>
+__device__ __forceinline__ void global_combine_max<double>(double *addr, double v)
+{
+    if (v > 0.0) {
+        atomicMax(reinterpret_cast<long long *>(addr), __double_as_longlong(v));
+    } else if (v == v) {
+        combine_max(addr, v);
+    }
+}
+
+/* ---- lines-strategy pixel enumeration ---------------------------------------------
+ * Work items are (line, kSeg-column segment) pairs, i.e. walk checkpoints.  A warp
+ * takes 32 of them from an atomic counter: every lane resumes its line's walk
+ * (bresenham.hpp:352-383 outer loop) from the checkpoint for kSeg columns into the
+ * warp's shared entries; the warp then flattens the spans of those entries into one
+ * pixel per lane (warp scan + shuffle binary search) and calls
+ *     act.pixel(p, line, slot, x, y, E, te, ne)
+ * for every pixel the reference draws (visited by the walk, error E <= 1, inside the
+ * frame), with act.item_begin(lane) / act.item_end(lane) around each warp item.  The
+ * forward, the max-overlap winner pass and the adjoint are such actions. */
+
+constexpr int kSegWarps = 4;
+
+/* what an action may need about the line of a slot */
+template <typename T>
+struct SlotLine {
+    long long fbase;    /* frame * H * W                        */
+    int line;           /* line index, -1 for an empty slot     */
+    T x0, y0, t0, t1, w;
+};
+
+template <typename T>
+struct DriveArgs {
+    const LineRec<T> *recs;
+    const Checkpoint<T> *cks;
+    int H, W;
+    DevStatus *st;
+    unsigned long long *work;      /* work-item counter, zeroed before the launch */
+};
+
+template <typename T, class Act>
+__device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
+{
+    using A = Ar<T>;
+    __shared__ Entry<T> ent_s[kSegWarps][32 * kSeg];
+    __shared__ SlotParams<T> prm_s[kSegWarps][32];
+    __shared__ SlotLine<T> sln_s[kSegWarps][32];
+    if (a.st->flags & kFatal) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Entry<T> *ent = ent_s[warp];
+    SlotParams<T> *prm = prm_s[warp];
+    SlotLine<T> *sln = sln_s[warp];
+    const long long total = (long long)a.st->cks;
+
+    for (;;) {
+        long long base = 0;
+        if (lane == 0) base = (long long)atomicAdd(a.work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const long long item = base + lane;
+        #pragma unroll
+        for (int k = 0; k < kSeg; k++) ent[lane * kSeg + k].c = kInvalidEntry;
+        sln[lane].line = -1;
+        if (item < total) {
+            const Checkpoint<T> ck = a.cks[item];
+            if (ck.cx != INT_MIN) {
+                const LineRec<T> r = a.recs[ck.line];
+                const int ax = r.flags & kAxisY;
+                Walker<T> wk;
+                wk.init(r);
+                wk.cx = ck.cx;
+                wk.cy = ck.cy;
+                wk.te = ck.te;
+                wk.ne = ck.ne;
+                const int sa = ax ? wk.sy : wk.sx;
+                const int lo = ck.seg * kSeg, hi = min(lo + kSeg - 1, r.ncols - 1);
+                SlotParams<T> p;
+                p.ts = ax ? r.t0 : r.t1;
+                p.ns = ax ? r.t1 : -r.t0;
+                p.len = r.len;
+                p.len2 = r.len2;
+                p.ww = r.ww;
+                p.rlen = r.rlen;
+                p.rww = r.rww;
+                p.ne_thr = r.ne_thr;
+                p.rns = 1.0f / (float)p.ns;
+                p.ss = ax ? wk.sx : wk.sy;
+                p.axis = ax;
+                p.fast = (r.flags & kFastDiv) ? 1 : 0;
+                prm[lane] = p;
+                SlotLine<T> sl;
+                sl.fbase = (long long)r.frame * a.H * a.W;
+                sl.line = ck.line;
+                sl.x0 = r.px;
+                sl.y0 = r.py;
+                sl.t0 = r.t0;
+                sl.t1 = r.t1;
+                sl.w = r.w;
+                sln[lane] = sl;
+                int guard = 0;
+                while (wk.cx != r.x1 && wk.cy != r.y1) {
+                    bool nx, ny;
+                    T exx;
+                    wk.decide(nx, ny, exx);
+                    const int c = ax ? wk.cy : wk.cx;
+                    const int idx = (c - r.c0) * sa;
+                    if (idx > hi) break;
+                    if ((ax ? ny : nx) && idx >= lo) {
+                        Entry<T> en;
+                        en.c = c;
+                        en.sc = ax ? wk.cx : wk.cy;
+                        en.te = wk.te;
+                        en.ne = wk.ne;
+                        ent[lane * kSeg + (idx - lo)] = en;
+                        if (idx == hi) break;
+                    }
+                    wk.step(nx, ny, exx);
+                    if (++guard > 4 * CBC_MAX_WALK + 64) {
+                        atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                        break;
+                    }
+                }
+            }
+        }
+        act.item_begin(lane);
+        __syncwarp();
+        #pragma unroll 1
+        for (int b = 0; b < kSeg; b++) {
+            const int e = b * 32 + lane;
+            int cnt = 0, jlo = 0;
+            {
+                const Entry<T> en = ent[e];
+                if (en.c != kInvalidEntry) {
+                    const SlotParams<T> &p = prm[e / kSeg];
+                    cnt = span_window(p, en.sc, en.ne, 0, (p.axis ? a.W : a.H) - 1, jlo);
+                }
+            }
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            const int excl = incl - cnt;
+            const int items = __shfl_sync(0xffffffffu, incl, 31);
+            for (int t0 = 0; t0 < items; t0 += 32) {
+                const int t = t0 + lane;
+                int o = 0;
+                #pragma unroll
+                for (int bit = 16; bit > 0; bit >>= 1) {
+                    const int v = __shfl_sync(0xffffffffu, excl, o + bit);
+                    if (v <= t) o += bit;
+                }
+                const int off_o = __shfl_sync(0xffffffffu, excl, o);
+                const int jlo_o = __shfl_sync(0xffffffffu, jlo, o);
+                if (t >= items) continue;
+                const int eo = b * 32 + o;
+                const int slot = eo / kSeg;
+                const Entry<T> en = ent[eo];
+                const SlotParams<T> &p = prm[slot];
+                const int j = jlo_o + (t - off_o);
+                T te = en.te, ne = en.ne;
+                bool visited = true;
+                if (j != 0) {
+                    const T dt = j > 0 ? p.ts : -p.ts, dn = j > 0 ? p.ns : -p.ns;
+                    te = A::add(te, dt);
+                    ne = A::add(ne, dn);
+                    visited = fabs(ne) < p.ne_thr;
+                    const int k = j > 0 ? j : -j;
+                    for (int q = 1; q < k; q++) {
+                        te = A::add(te, dt);
+                        ne = A::add(ne, dn);
+                    }
+                    visited = visited && fabs(ne) < p.ne_thr;
+                }
+                if (!visited) continue;
+                const T nf = A::nterm(ne, p);
+                const T E = A::error(te, nf, p);
+                if (!(E <= T(1))) continue;
+                const int y = en.sc + j;
+                const int px = p.axis ? y : en.c, py = p.axis ? en.c : y;
+                act.pixel(p, sln[slot], slot, px, py, E, te, ne);
+            }
+        }
+        __syncwarp();
+        act.item_end(lane, sln[lane]);
+        __syncwarp();
+    }
+}
+
+/* host-side error reporting, defined in cbc_draw_lines.cu */
+int fail(int code, const std::string &msg);
+void clear_error();
+
+}  // namespace cbc
+
+#endif /* CBC_COMMON_CUH */

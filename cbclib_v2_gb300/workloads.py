@@ -80,3 +80,26 @@ def frames_subset(ls: LineSet, frames) -> LineSet:
     idxs = np.array([remap[int(f)] for f in ls.idxs[sel]], dtype=np.int64)
     return LineSet(ls.name + '_subset', (len(frames), ls.shape[1], ls.shape[2]),
                    ls.lines[sel], idxs, ls.kernel, ls.overlap, ls.max_val)
+
+
+def fit_stack(seed: int = 0, F: int = 8, H: int = 1024, W: int = 1024,
+              per_frame: int = 5000) -> LineSet:
+    """8 frames of 1024x1024 with 5,000 segments each, distributed as in the
+    single-frame workload; biweight profile (C1, so gradients are meaningful), sum
+    overlap.  max_val puts a single line's peak at 100 counts."""
+    rng = np.random.default_rng(seed)
+    n = F * per_frame
+    lines = _segments(rng, n, H, W, rng.uniform(10, 100, n), rng.uniform(1, 5, n))
+    idxs = np.repeat(np.arange(F, dtype=np.int64), per_frame)
+    return LineSet(f'fit_stack_{F}x{H}x{W}', (F, H, W), lines, idxs, 'biweight', 'sum',
+                   max_val=100.0 / 0.9375)
+
+
+def perturbed(lines: np.ndarray, seed: int, sigma_pt: float = 0.5,
+              sigma_w: float = 0.2) -> np.ndarray:
+    """lines with endpoints moved by N(0, sigma_pt) and widths by N(0, sigma_w)"""
+    rng = np.random.default_rng(seed)
+    out = lines.copy()
+    out[:, :4] += rng.normal(0.0, sigma_pt, (lines.shape[0], 4))
+    out[:, 4] = np.maximum(out[:, 4] + rng.normal(0.0, sigma_w, lines.shape[0]), 0.5)
+    return out

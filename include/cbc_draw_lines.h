@@ -142,6 +142,39 @@ CBC_API int cbc_draw_lines_f32_noalloc(float *out, int64_t n_frames, int64_t hei
                                        const void *idxs, int32_t idx_bytes, float max_val,
                                        int32_t kernel, int32_t overlap, void *stream);
 
+/* ---- adjoint (no counterpart in the reference) ----------------------------------
+ * Gradient of draw_lines with respect to the line parameters, from the gradient of
+ * the frames: grad_lines[i] = sum over the pixels p line i draws of
+ * grad_out[p] * d(max_val K(d(p)/w))/d(x0, y0, x1, y1, w), over exactly the pixels the
+ * forward draws.  For max overlap only the line whose value a pixel kept receives
+ * that pixel's gradient: pass the forward's result `image`, the frames before drawing
+ * `out0` (NULL: zeros) and a (n_frames, height, width) int32 `winner` buffer, which
+ * comes back holding each pixel's winning line (0x7f7f7f7f where none drew the value).
+ * `grad_lines` (n_lines, 5) is overwritten.  Device-detected errors are reported
+ * through the workspace status as for cbc_draw_lines_*; capacity and walk limits as
+ * there. */
+CBC_API size_t cbc_draw_lines_backward_workspace_size(int64_t n_lines,
+                                                      int64_t checkpoint_capacity,
+                                                      int32_t elem_bytes);
+
+CBC_API int cbc_draw_lines_backward_f32(const float *grad_out, int64_t n_frames,
+                                        int64_t height, int64_t width, const float *lines,
+                                        int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                        float max_val, int32_t kernel, int32_t overlap,
+                                        const float *image, const float *out0,
+                                        int32_t *winner, float *grad_lines, void *workspace,
+                                        size_t workspace_bytes, int64_t checkpoint_capacity,
+                                        void *stream);
+
+CBC_API int cbc_draw_lines_backward_f64(const double *grad_out, int64_t n_frames,
+                                        int64_t height, int64_t width, const double *lines,
+                                        int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                        double max_val, int32_t kernel, int32_t overlap,
+                                        const double *image, const double *out0,
+                                        int32_t *winner, double *grad_lines, void *workspace,
+                                        size_t workspace_bytes, int64_t checkpoint_capacity,
+                                        void *stream);
+
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
 CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
