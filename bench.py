@@ -46,9 +46,11 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--workload', default='detector_stack',
-                   choices=['detector_stack', 'fit'],
+                   choices=['detector_stack', 'fit', 'ragged'],
                    help='detector_stack: the headline forward; fit: forward + adjoint '
-                        'iterations on 8 x 1024^2 frames vs a finite-difference gradient')
+                        'iterations on 8 x 1024^2 frames vs a finite-difference gradient; '
+                        'ragged: 256 x 1024^2 frames with lognormal line counts, one '
+                        'CUDA-graph launch vs per-frame plain launches')
     return p.parse_args()
 
 
@@ -250,11 +252,66 @@ def run_fit(args, world, rank, local):
             'loss': float(loss.item())}), flush=True)
 
 
+def run_ragged(args, world, rank, local):
+    """256 frames of 1024^2, lognormal(median 1,500, sigma 1) segments per frame clipped
+    to [100, 20,000], triangular, sum: one graph replay of the autotuned CSR draw per
+    step, against one public draw_lines call per frame"""
+    import torch
+    from cbclib_v2_gb300 import batch, workloads
+    torch.cuda.set_device(local)
+    ls = workloads.ragged_stack(seed=3000 + rank)
+    offs = ls.frame_offsets()
+    lines = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    r = batch.RaggedRenderer(ls.shape, offs, max_val=ls.max_val, kernel=ls.kernel,
+                             overlap=ls.overlap)
+    r(lines)
+    r.check()
+    for _ in range(args.warmup):
+        r.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        r.replay()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms_graph = a.elapsed_time(b) / args.steps
+    r.check()
+    out = torch.zeros(ls.shape, device='cuda')
+    batch.render_per_frame(out, lines, offs, ls.max_val, ls.kernel, ls.overlap)
+    torch.cuda.synchronize()
+    k = max(2, args.steps // 5)
+    a.record(stream)
+    for _ in range(k):
+        batch.render_per_frame(out, lines, offs, ls.max_val, ls.kernel, ls.overlap)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms_frames = a.elapsed_time(b) / k
+    t = r.tuning
+    if rank == 0:
+        print(json.dumps({
+            'metric': 'ragged draw_lines throughput', 'value': world * ls.n_lines / ms_graph / 1e3,
+            'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms_graph, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+                       'lines_per_frame_min_max': [int(np.diff(offs).min()), int(np.diff(offs).max())],
+                       'kernel': ls.kernel, 'overlap': ls.overlap},
+            'autotuned': {f: getattr(t, f) for f, _ in type(t)._fields_} if t is not None else None,
+            'autotune_ms': r.timings,
+            'per_frame_launches_ms': ms_frames,
+            'graph_speedup_vs_per_frame': ms_frames / ms_graph}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
     if args.workload == 'fit' and args.impl == 'gb300':
         run_fit(args, world, rank, local)
+        return
+    if args.workload == 'ragged' and args.impl == 'gb300':
+        run_ragged(args, world, rank, local)
         return
     import torch
     from cbclib_v2_gb300 import _native, draw_lines, workloads

@@ -48,6 +48,7 @@ _lib = None
 
 # every symbol declared in include/cbc_draw_lines.h
 EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_lines_f64',
+           'cbc_draw_lines_csr_f32', 'cbc_draw_lines_csr_f64',
            'cbc_draw_lines_f32_noalloc', 'cbc_draw_lines_backward_workspace_size',
            'cbc_draw_lines_backward_f32', 'cbc_draw_lines_backward_f64', 'cbc_read_status',
            'cbc_profile_enable', 'cbc_profile_read', 'cbc_last_error', 'cbc_version')
@@ -67,6 +68,11 @@ def _declare(lib):
         f = getattr(lib, 'cbc_draw_lines_' + sfx)
         f.argtypes = [p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, ctypes.c_size_t,
                       i64, i64, ctypes.POINTER(Tuning), p]
+        f.restype = ctypes.c_int
+    for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
+        f = getattr(lib, 'cbc_draw_lines_csr_' + sfx)
+        f.argtypes = [p, i64, i64, i64, p, i64, p, real, i32, i32, p, ctypes.c_size_t, i64, i64,
+                      ctypes.POINTER(Tuning), p]
         f.restype = ctypes.c_int
     lib.cbc_draw_lines_f32_noalloc.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
                                                i32, i32, p]

@@ -404,7 +404,7 @@ struct CallTimer {
 };
 
 struct Layout {
-    size_t status, recs, counts, offsets, fillpos, pairs, cks, total;
+    size_t status, recs, counts, offsets, fillpos, pairs, cks, frames, total;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -447,6 +447,7 @@ Layout make_layout(long long n_frames, long long H, long long W, long long n_lin
     L.recs = off;    off = align_up(off + rec_bytes * (size_t)n_lines, 256);
     L.pairs = off;   off = align_up(off + sizeof(int) * (size_t)capacity, 256);
     L.cks = off;     off = align_up(off + ck_bytes * (size_t)ck_capacity, 256);
+    L.frames = off;  off = align_up(off + sizeof(int) * (size_t)n_lines, 256);
     L.total = off;
     return L;
 }
@@ -515,6 +516,31 @@ cudaError_t launch_segments_k(const SegArgs<T> &sa, int kernel, int overlap, cud
     }
 }
 
+/* CSR frame offsets -> one int32 frame index per line (binary search), with the
+ * offsets' rules checked on the device */
+__global__ void __launch_bounds__(kThreads)
+csr_frames_kernel(const int64_t *__restrict__ offs, long long n_frames, long long n_lines,
+                  int *__restrict__ frames, DevStatus *st)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= n_frames) {
+        const long long o = offs[i];
+        bool bad = (i == 0 && o != 0) || (i == n_frames && o != n_lines) ||
+                   (i < n_frames && offs[i + 1] < o);
+        if (bad) {
+            atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
+            atomicMin(&st->bad_line, (unsigned long long)i);
+        }
+    }
+    if (i >= n_lines) return;
+    long long lo = 0, hi = n_frames;          /* last f with offs[f] <= i */
+    while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (offs[mid] <= i) lo = mid; else hi = mid;
+    }
+    frames[i] = (int)lo;
+}
+
 /* lines per megapixel below which warps of lines beat (frame, tile) bins */
 constexpr double kLinesDensity = 1000.0;
 
@@ -522,7 +548,8 @@ template <typename T>
 int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const T *lines,
                     long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel,
                     int overlap, void *workspace, size_t ws_bytes, long long capacity,
-                    long long ck_capacity, const cbc_tuning *tuning, void *stream)
+                    long long ck_capacity, const cbc_tuning *tuning, void *stream,
+                    const int64_t *csr = nullptr)
 {
     g_error.clear();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
@@ -534,7 +561,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
         return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
     if (idxs && idx_bytes != 4 && idx_bytes != 8)
         return fail(CBC_ERR_INVALID, "idx_bytes must be 4 or 8");
-    if (!idxs && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
+    if (!idxs && !csr && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
         return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
                                          " != " + std::to_string(n_frames) + ")");
     if (n_lines > 0 && (!out || !lines) && n_frames * H * W > 0)
@@ -558,6 +585,16 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     timer.mark(0);
     init_status_kernel<<<1, 1, 0, s>>>(st);
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && csr) {
+        if (n_frames > INT_MAX) return fail(CBC_ERR_INVALID, "too many frames");
+        int *fr = reinterpret_cast<int *>(ws + L.frames);
+        const long long m = (n_lines > n_frames ? n_lines : n_frames + 1);
+        csr_frames_kernel<<<(unsigned)((m + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+            csr, n_frames, n_lines, fr, st);
+        e = cudaGetLastError();
+        idxs = fr;
+        idx_bytes = 4;
+    }
     Geometry g;
     g.H = (int)H;
     g.W = (int)W;
@@ -693,6 +730,32 @@ int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, int64_t wi
                                         idx_bytes, max_val, kernel, overlap, workspace,
                                         workspace_bytes, pair_capacity, checkpoint_capacity,
                                         tuning, stream);
+}
+
+int cbc_draw_lines_csr_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
+                           const float *lines, int64_t n_lines, const int64_t *frame_offsets,
+                           float max_val, int32_t kernel, int32_t overlap, void *workspace,
+                           size_t workspace_bytes, int64_t pair_capacity,
+                           int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
+{
+    if (!frame_offsets) return cbc::fail(CBC_ERR_INVALID, "null frame_offsets");
+    return cbc::draw_lines_impl<float>(out, n_frames, height, width, lines, n_lines, nullptr, 0,
+                                       max_val, kernel, overlap, workspace, workspace_bytes,
+                                       pair_capacity, checkpoint_capacity, tuning, stream,
+                                       frame_offsets);
+}
+
+int cbc_draw_lines_csr_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
+                           const double *lines, int64_t n_lines, const int64_t *frame_offsets,
+                           double max_val, int32_t kernel, int32_t overlap, void *workspace,
+                           size_t workspace_bytes, int64_t pair_capacity,
+                           int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
+{
+    if (!frame_offsets) return cbc::fail(CBC_ERR_INVALID, "null frame_offsets");
+    return cbc::draw_lines_impl<double>(out, n_frames, height, width, lines, n_lines, nullptr, 0,
+                                        max_val, kernel, overlap, workspace, workspace_bytes,
+                                        pair_capacity, checkpoint_capacity, tuning, stream,
+                                        frame_offsets);
 }
 
 int cbc_read_status(const void *workspace, cbc_status *status, void *stream)

@@ -17,7 +17,7 @@ import torch
 from . import _native
 from . import device as _device
 
-__all__ = ['draw_lines', 'Workspace', 'tuning']
+__all__ = ['draw_lines', 'draw_lines_csr', 'Workspace', 'tuning']
 
 _tls = threading.local()
 
@@ -121,26 +121,25 @@ def _raise_rc(rc: int):
     raise RuntimeError(f"cbc_draw_lines failed ({rc}): {msg}")
 
 
-def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int,
-                     overlap: int, tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
-    if out.dtype not in (torch.float32, torch.float64):
-        raise TypeError(f"out must be float32 or float64, got {out.dtype}")
+def _resolve_tuning(tuning, out: torch.Tensor, n_lines: int, kernel: int, overlap: int):
+    """forced tuning > this thread's `tuning(...)` block > autotuned choice > default"""
     if tuning is None:
         tuning = getattr(_tls, 'tuning', None)
-    if out.dim() < 2:
-        raise ValueError("Output array has insufficient number of dimensions")
-    dev = out.device
-    ln = _as_device_lines(lines, dev, out.dtype)
-    n_lines = ln.shape[0]
-    ix = _as_device_idxs(idxs, n_lines, dev)
-    H, W = int(out.shape[-2]), int(out.shape[-1])
-    F = math.prod(int(s) for s in out.shape[:-2])
-    if ix is None and n_lines and F != 1 and F != n_lines:
-        raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
-    work = out if out.is_contiguous() else out.contiguous()
+    if tuning is None:
+        from . import autotune
+        names = {v: k for k, v in _native.KERNELS.items()}
+        ovn = {v: k for k, v in _native.OVERLAPS.items()}
+        tuning = autotune.lookup(autotune.workload_key(out.shape, out.dtype, names[kernel],
+                                                       ovn[overlap], n_lines, out.device))
+    return tuning
+
+
+def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines: int,
+                        elem: int, tuning) -> None:
+    """Run `call(buf, nbytes, capacity, ck_capacity, tref, stream)` with this thread's
+    workspace, read the status, raise the reference's errors and repeat with a larger
+    workspace when the call reports that its pairs or checkpoints did not fit."""
     lib = _native.lib()
-    elem = 4 if out.dtype == torch.float32 else 8
-    fn = lib.cbc_draw_lines_f32 if elem == 4 else lib.cbc_draw_lines_f64
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev)
         ws = _workspace(dev, stream)
@@ -153,11 +152,7 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
             if nbytes == 0:
                 raise ValueError(_native.last_error() or "invalid sizes or tuning")
             buf = ws.ensure(nbytes)
-            rc = fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines,
-                    None if ix is None else ix.data_ptr(),
-                    0 if ix is None else ix.element_size(), max_val, kernel, overlap,
-                    buf.data_ptr(), buf.numel(), capacity, ck_capacity, tref,
-                    stream.cuda_stream)
+            rc = call(buf, capacity, ck_capacity, tref, stream.cuda_stream)
             if rc:
                 _raise_rc(rc)
             st = _native.Status()
@@ -168,13 +163,77 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
             if not st.has(_native.CBC_ERR_CAPACITY):
                 ws.capacity = capacity
                 ws.ck_capacity = ck_capacity
-                break
+                return
             capacity = max(capacity, int(st.pairs_needed * 1.25) + 1024)
             ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
             if capacity > 2**31 - 1 or ck_capacity > 2**31 - 1:
                 raise MemoryError("too many (line, tile) pairs or walk checkpoints for one call")
-        else:
-            raise RuntimeError("pair capacity did not converge")
+    raise RuntimeError("workspace capacity did not converge")
+
+
+def _frames_of(out: torch.Tensor):
+    if out.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"out must be float32 or float64, got {out.dtype}")
+    if out.dim() < 2:
+        raise ValueError("Output array has insufficient number of dimensions")
+    H, W = int(out.shape[-2]), int(out.shape[-1])
+    F = math.prod(int(s) for s in out.shape[:-2])
+    return F, H, W
+
+
+def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int,
+                     overlap: int, tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
+    F, H, W = _frames_of(out)
+    dev = out.device
+    ln = _as_device_lines(lines, dev, out.dtype)
+    n_lines = ln.shape[0]
+    ix = _as_device_idxs(idxs, n_lines, dev)
+    if ix is None and n_lines and F != 1 and F != n_lines:
+        raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
+    tuning = _resolve_tuning(tuning, out, n_lines, kernel, overlap)
+    work = out if out.is_contiguous() else out.contiguous()
+    elem = 4 if out.dtype == torch.float32 else 8
+    lib = _native.lib()
+    fn = lib.cbc_draw_lines_f32 if elem == 4 else lib.cbc_draw_lines_f64
+
+    def call(buf, capacity, ck_capacity, tref, stream):
+        return fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines,
+                  None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                  max_val, kernel, overlap, buf.data_ptr(), buf.numel(), capacity, ck_capacity,
+                  tref, stream)
+
+    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning)
+    if work is not out:
+        out.copy_(work)
+    return out
+
+
+def draw_lines_csr(out: torch.Tensor, lines, frame_offsets, max_val: float = 1.0,
+                   kernel: str = 'rectangular', overlap: str = 'sum',
+                   tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
+    """draw_lines for a ragged stack whose lines are grouped by frame: frame f owns
+    lines[frame_offsets[f]:frame_offsets[f + 1]] (int64 CSR offsets, F + 1 entries).
+    ``out`` is a CUDA tensor (..., H, W) updated in place."""
+    k, ov = _check_names(kernel, overlap)
+    F, H, W = _frames_of(out)
+    dev = out.device
+    ln = _as_device_lines(lines, dev, out.dtype)
+    n_lines = ln.shape[0]
+    offs = torch.as_tensor(frame_offsets).to(device=dev, dtype=torch.int64).reshape(-1)
+    if offs.numel() != F + 1:
+        raise ValueError(f"frame_offsets has {offs.numel()} entries, expected {F + 1}")
+    offs = offs.contiguous()
+    tuning = _resolve_tuning(tuning, out, n_lines, k, ov)
+    work = out if out.is_contiguous() else out.contiguous()
+    elem = 4 if out.dtype == torch.float32 else 8
+    lib = _native.lib()
+    fn = lib.cbc_draw_lines_csr_f32 if elem == 4 else lib.cbc_draw_lines_csr_f64
+
+    def call(buf, capacity, ck_capacity, tref, stream):
+        return fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines, offs.data_ptr(), max_val, k,
+                  ov, buf.data_ptr(), buf.numel(), capacity, ck_capacity, tref, stream)
+
+    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning)
     if work is not out:
         out.copy_(work)
     return out

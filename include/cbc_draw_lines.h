@@ -111,6 +111,26 @@ CBC_API int cbc_draw_lines_f64(double *out, int64_t n_frames, int64_t height, in
                                int64_t pair_capacity, int64_t checkpoint_capacity,
                                const cbc_tuning *tuning, void *stream);
 
+/* Ragged stacks: the lines are grouped by frame and frame f owns lines
+ * [frame_offsets[f], frame_offsets[f + 1]) (int64 CSR offsets, n_frames + 1 entries,
+ * frame_offsets[0] == 0, frame_offsets[n_frames] == n_lines).  Otherwise as
+ * cbc_draw_lines_f32 / _f64; offsets that break those rules are a device-detected
+ * CBC_ERR_INDEX.  The call launches a fixed sequence of kernels and memsets and reads
+ * nothing back, so it can be captured into a CUDA graph and replayed. */
+CBC_API int cbc_draw_lines_csr_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
+                                   const float *lines, int64_t n_lines,
+                                   const int64_t *frame_offsets, float max_val, int32_t kernel,
+                                   int32_t overlap, void *workspace, size_t workspace_bytes,
+                                   int64_t pair_capacity, int64_t checkpoint_capacity,
+                                   const cbc_tuning *tuning, void *stream);
+
+CBC_API int cbc_draw_lines_csr_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
+                                   const double *lines, int64_t n_lines,
+                                   const int64_t *frame_offsets, double max_val, int32_t kernel,
+                                   int32_t overlap, void *workspace, size_t workspace_bytes,
+                                   int64_t pair_capacity, int64_t checkpoint_capacity,
+                                   const cbc_tuning *tuning, void *stream);
+
 /* Limits of cbc_draw_lines_f32_noalloc. */
 #define CBC_NOALLOC_MAX_LINES       16384
 #define CBC_NOALLOC_MAX_CHECKPOINTS 262144
