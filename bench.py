@@ -8,9 +8,13 @@ indices): one step = one draw_lines call over the whole stack.
 Prints one JSON line (rank 0).  `value` is device-resident throughput in Mlines/s
 (lines, indices and frames already in HBM); `e2e` is the same metric through the
 public API with pinned host buffers (frames, lines and indices copied in, frames
-copied out every step).  `roofline` is the render kernel's achieved HBM bandwidth
-from CUDA events recorded on its stream around every launch in the timed region,
-with the read-modify-write byte count 2*F*H*W*4 + N*24 per launch.  `cpu_baseline`
+copied out every step).  `roofline` is the dominant kernel's achieved HBM bandwidth
+(segments_kernel or render_kernel, whichever strategy the call ran) from CUDA events
+recorded on its stream around every launch in the timed region; its byte count is a
+read and a write of every 32-byte sector of the output that holds a drawn pixel plus
+24 bytes per line (the full-frame read-modify-write, 2*F*H*W*4 + N*24, is reported
+beside it as `full_frame_rmw_frac`).  `gpu_launches` is the library's own count of
+the kernels it launched in the timed region.  `cpu_baseline`
 times the oracle (C port of the reference CPU rasteriser) on a bounded sample with
 all host threads.  Under torchrun each rank renders its own stack (weak scaling, no
 collective on the data path).  `--impl reference` times the reference CPU algorithm
@@ -31,13 +35,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
-KERNELS_PER_CALL = 5          # init_status, prep, offsets, fill, render
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument('--gpus', type=int, default=1)
-    p.add_argument('--steps', type=int, default=20)
+    p.add_argument('--steps', type=int, default=1000)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--frames', type=int, default=64)
@@ -62,7 +65,8 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms; only the samples taken
+    between begin() and end() (the timed region) are reported."""
     FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
               'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
               'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
@@ -71,20 +75,32 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.window = (0.0, float('inf'))
 
     def start(self):
+        """start sampling and wait (at most 10 s) for the first sample"""
         try:
             self.proc = subprocess.Popen(
                 ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
-                 '-lms', '200', '-i', str(self.gpu)], stdout=subprocess.PIPE,
+                 '-lms', '100', '-i', str(self.gpu)], stdout=subprocess.PIPE,
                 stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except (OSError, ValueError):
             self.proc = None
+            return
+        t_end = time.perf_counter() + 10.0
+        while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def begin(self):
+        self.window = (time.perf_counter(), float('inf'))
+
+    def end(self):
+        self.window = (self.window[0], time.perf_counter())
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def stop(self):
         if self.proc is None:
@@ -96,7 +112,10 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        for ln in self.lines:
+        lo, hi = self.window
+        for t, ln in self.lines:
+            if not lo <= t <= hi:
+                continue
             f = [x.strip() for x in ln.split(',')]
             if len(f) < 9:
                 continue
@@ -122,14 +141,15 @@ def measured_peak():
         return FALLBACK_HBM_GBS, 'fallback'
 
 
-def committed_traffic(workload: str):
-    """DRAM bytes per render launch from the committed ncu summary, or None."""
+def committed_traffic(workload: str, kernel: str):
+    """DRAM bytes (read + write) per launch of `kernel` on `workload` from the committed
+    ncu summary, or None."""
     path = os.path.join(ROOT, 'profiles', 'render_traffic.json')
     try:
         with open(path) as fh:
             d = json.load(fh)
-        return d.get(workload)
-    except (OSError, ValueError):
+        return d.get(workload, {}).get(kernel)
+    except (OSError, ValueError, AttributeError):
         return None
 
 
@@ -314,7 +334,7 @@ def main():
         run_ragged(args, world, rank, local)
         return
     import torch
-    from cbclib_v2_gb300 import _native, draw_lines, workloads
+    from cbclib_v2_gb300 import _native, draw_lines, ndimage, workloads
 
     ls = workloads.detector_stack(seed=1000 + rank, F=args.frames)
     if args.impl == 'reference':
@@ -349,13 +369,16 @@ def main():
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
     t0.record(stream)
     for _ in range(args.steps):
         draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
     t1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     barrier()
     prof = _native.profile_read(reset=True)
+    strategy = ndimage.last_status(dev).strategy
     _native.profile_enable(False)
     clk = clocks.stop()
     ms = t0.elapsed_time(t1)
@@ -374,7 +397,7 @@ def main():
         h_idxs = torch.from_numpy(ls.idxs.astype(np.int32)).pin_memory()
         for _ in range(max(1, args.warmup)):
             draw_lines(h_out, h_lines, h_idxs, ls.max_val, ls.kernel, ls.overlap)
-        e_steps = max(3, args.steps // 4)
+        e_steps = max(3, min(args.steps // 4, 50))
         barrier()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -401,6 +424,7 @@ def main():
 
     peak, peak_src = measured_peak()
     render_ms = prof.ms_render / max(prof.calls, 1)
+    kname = 'segments_kernel' if strategy == _native.STRATEGY_LINES else 'render_kernel'
     # bytes the op must move: every 32-byte sector of `out` holding a drawn pixel is
     # read and written once (all other sectors are untouched), plus each line's
     # 5 coordinates and frame index
@@ -410,7 +434,7 @@ def main():
     achieved = algo_bytes / (render_ms * 1e-3) / 1e9
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_src,
-                'traffic': committed_traffic(ls.name), 'kernel': 'render_kernel',
+                'traffic': committed_traffic(ls.name, kname), 'kernel': kname,
                 'algorithmic_bytes': algo_bytes,
                 'bytes_model': 'read+write of each 32 B sector holding a drawn pixel '
                                '(%d of %d sectors) + 24 B per line' % (drawn_sectors, F * H * W // 8),
@@ -427,7 +451,7 @@ def main():
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
         'data': 'synthetic', 'config': workload_config(ls), 'roofline': roofline,
         'output_gbs': F * H * W * 4 / (ms_step * 1e-3) / 1e9, 'clocks': clk,
-        'gpu_launches': KERNELS_PER_CALL * args.steps, 'e2e': e2e,
+        'gpu_launches': prof.launches, 'e2e': e2e,
     }
     if not args.no_cpu_baseline and world == 1:
         res['cpu_baseline'] = cpu_baseline(ls, args.cpu_frames)

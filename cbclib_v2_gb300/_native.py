@@ -27,7 +27,7 @@ class Tuning(ctypes.Structure):
 
 class Status(ctypes.Structure):
     """cbc_status: device-side result flags of the last call on a workspace."""
-    _fields_ = [('flags', ctypes.c_int32), ('reserved', ctypes.c_int32),
+    _fields_ = [('flags', ctypes.c_int32), ('strategy', ctypes.c_int32),
                 ('bad_line', ctypes.c_int64), ('idx_min', ctypes.c_int64),
                 ('idx_max', ctypes.c_int64), ('pairs_needed', ctypes.c_int64),
                 ('checkpoints_needed', ctypes.c_int64)]
@@ -38,7 +38,7 @@ class Status(ctypes.Structure):
 
 class Profile(ctypes.Structure):
     """cbc_profile: accumulated per-stage device milliseconds of profiled calls."""
-    _fields_ = [('calls', ctypes.c_int32), ('reserved', ctypes.c_int32),
+    _fields_ = [('calls', ctypes.c_int32), ('launches', ctypes.c_int32),
                 ('ms_prep', ctypes.c_double), ('ms_offsets', ctypes.c_double),
                 ('ms_fill', ctypes.c_double), ('ms_render', ctypes.c_double)]
 

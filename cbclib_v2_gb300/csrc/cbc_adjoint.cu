@@ -175,6 +175,7 @@ cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, int grid, cudaStre
 {
     if (overlap == CBC_MAX) {
         winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
+        note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
@@ -183,6 +184,7 @@ cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, int grid, cudaStre
     } else {
         backward_kernel<T, K, CBC_SUM><<<grid, kSegWarps * 32, 0, s>>>(aa);
     }
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -224,7 +226,8 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
     Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
     double *gacc = reinterpret_cast<double *>(ws + L.gacc);
-    init_status_kernel<<<1, 1, 0, s>>>(st);
+    init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);
+    note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines == 0) return CBC_OK;
@@ -242,6 +245,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     else
         prep_kernel<T, int32_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
                                                                 recs, nullptr, cks, ck_capacity, st);
+    note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (pixels) {
@@ -277,6 +281,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     }
     const long long n5 = 5 * n_lines;
     finalize_kernel<T><<<(unsigned)((n5 + 255) / 256), 256, 0, s>>>(gacc, grad_lines, n5);
+    note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     return CBC_OK;

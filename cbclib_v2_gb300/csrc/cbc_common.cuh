@@ -62,7 +62,7 @@ struct Checkpoint {
 /* status block at the start of the workspace */
 struct DevStatus {
     int flags;
-    int reserved;
+    int strategy;                  /* CBC_STRATEGY_TILES / _LINES of the call */
     unsigned long long bad_line;
     long long idx_min;
     long long idx_max;
@@ -437,10 +437,10 @@ prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lon
     recs[i] = r;
 }
 
-static __global__ void init_status_kernel(DevStatus *st)
+static __global__ void init_status_kernel(DevStatus *st, int strategy)
 {
     st->flags = 0;
-    st->reserved = 0;
+    st->strategy = strategy;
     st->bad_line = ~0ull >> 1;
     st->idx_min = LLONG_MAX;
     st->idx_max = LLONG_MIN;
@@ -853,6 +853,8 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
 /* host-side error reporting, defined in cbc_draw_lines.cu */
 int fail(int code, const std::string &msg);
 void clear_error();
+/* adds n to the library's kernel-launch counter (reported by cbc_profile_read) */
+void note_launches(int n);
 
 }  // namespace cbc
 

@@ -29,6 +29,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <string>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -354,6 +355,10 @@ int fail(int code, const std::string &msg)
 
 void clear_error() { g_error.clear(); }
 
+std::atomic<int> g_launches{0};
+
+void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 /* opt-in per-stage event timing */
 struct Profiler {
     std::mutex mu;
@@ -463,6 +468,7 @@ cudaError_t launch_render(const RenderArgs<T> &ra, long long n_bins, size_t smem
         if (e != cudaSuccess) return e;
     }
     fn<<<(unsigned)n_bins, threads, smem, s>>>(ra);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -494,6 +500,7 @@ cudaError_t launch_segments(const SegArgs<T> &sa, cudaStream_t s)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     segments_kernel<T, K, OV><<<(unsigned)(sms > 0 ? sms * 9 : 1024), kSegWarps * 32, 0, s>>>(sa);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -581,9 +588,16 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     unsigned char *ws = static_cast<unsigned char *>(workspace);
     DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    int strategy = t.strategy;
+    if (strategy == CBC_STRATEGY_AUTO) {
+        double mpx = (double)n_frames * (double)H * (double)W / 1e6;
+        strategy = (mpx > 0.0 && (double)n_lines / mpx < kLinesDensity) ? CBC_STRATEGY_LINES
+                                                                         : CBC_STRATEGY_TILES;
+    }
     CallTimer timer(s);
     timer.mark(0);
-    init_status_kernel<<<1, 1, 0, s>>>(st);
+    init_status_kernel<<<1, 1, 0, s>>>(st, strategy);
+    note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && csr) {
         if (n_frames > INT_MAX) return fail(CBC_ERR_INVALID, "too many frames");
@@ -591,6 +605,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
         const long long m = (n_lines > n_frames ? n_lines : n_frames + 1);
         csr_frames_kernel<<<(unsigned)((m + kThreads - 1) / kThreads), kThreads, 0, s>>>(
             csr, n_frames, n_lines, fr, st);
+        note_launches(1);
         e = cudaGetLastError();
         idxs = fr;
         idx_bytes = 4;
@@ -607,12 +622,6 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines == 0) return CBC_OK;
     unsigned nb_lines = (unsigned)((n_lines + kThreads - 1) / kThreads);
-    int strategy = t.strategy;
-    if (strategy == CBC_STRATEGY_AUTO) {
-        double mpx = (double)n_frames * (double)H * (double)W / 1e6;
-        strategy = (mpx > 0.0 && (double)n_lines / mpx < kLinesDensity) ? CBC_STRATEGY_LINES
-                                                                         : CBC_STRATEGY_TILES;
-    }
     LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
     Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
     const bool wide = idxs && idx_bytes == 8;
@@ -621,6 +630,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
                       lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
         else      prep_kernel<T, int32_t, false, true><<<nb_lines, kThreads, 0, s>>>(
                       lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
+        note_launches(1);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         timer.mark(1);
@@ -652,6 +662,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     else
         prep_kernel<T, int64_t, true, false><<<nb_lines, kThreads, 0, s>>>(
             lines, idxs, n_lines, n_frames, g, recs, counts, cks, ck_capacity, st);
+    note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_bins == 0) return CBC_OK;
@@ -664,6 +675,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     timer.mark(2);
     fill_kernel<T><<<nb_lines, kThreads, 0, s>>>(recs, n_lines, g, fillpos, pairs, capacity, cks,
                                                  st);
+    note_launches(2);
     timer.mark(3);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
@@ -768,7 +780,7 @@ int cbc_read_status(const void *workspace, cbc_status *status, void *stream)
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     status->flags = d.flags;
-    status->reserved = 0;
+    status->strategy = d.strategy;
     status->bad_line = (int64_t)d.bad_line;
     status->idx_min = d.idx_min;
     status->idx_max = d.idx_max;
@@ -804,13 +816,14 @@ int cbc_profile_read(cbc_profile *profile, int32_t reset)
     p.pending.clear();
     if (profile) {
         profile->calls = p.calls;
-        profile->reserved = 0;
+        profile->launches = cbc::g_launches.load();
         profile->ms_prep = p.ms[0];
         profile->ms_offsets = p.ms[1];
         profile->ms_fill = p.ms[2];
         profile->ms_render = p.ms[3];
     }
     if (reset) {
+        cbc::g_launches.store(0);
         p.calls = 0;
         for (double &m : p.ms) m = 0.0;
     }
@@ -892,7 +905,8 @@ int draw_lines_noalloc(float *out, long long n_frames, long long H, long long W,
     DevStatus *st = reinterpret_cast<DevStatus *>(base);
     LineRec<float> *recs = reinterpret_cast<LineRec<float> *>(base + kNoallocRecOffset);
     Checkpoint<float> *cks = reinterpret_cast<Checkpoint<float> *>(base + kNoallocCkOffset);
-    init_status_kernel<<<1, 1, 0, s>>>(st);        /* every call starts from a clean status */
+    init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);  /* a clean status per call */
+    note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines > 0) {
@@ -910,6 +924,7 @@ int draw_lines_noalloc(float *out, long long n_frames, long long H, long long W,
             prep_kernel<float, int32_t, false, true><<<nb, kThreads, 0, s>>>(
                 lines, idxs, n_lines, n_frames, g, recs, nullptr, cks,
                 CBC_NOALLOC_MAX_CHECKPOINTS, st);
+        note_launches(1);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         if (n_frames * H * W > 0) {

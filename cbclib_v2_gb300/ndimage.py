@@ -50,6 +50,7 @@ class Workspace:
         self.buffer: Optional[torch.Tensor] = None
         self.capacity = 0
         self.ck_capacity = 0
+        self.last_status: Optional[_native.Status] = None
 
     def ensure(self, nbytes: int) -> torch.Tensor:
         if self.buffer is None or self.buffer.numel() < nbytes:
@@ -159,6 +160,7 @@ def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines
             rc = lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream)
             if rc:
                 _raise_rc(rc)
+            ws.last_status = st
             _raise_status(st, F)
             if not st.has(_native.CBC_ERR_CAPACITY):
                 ws.capacity = capacity
@@ -169,6 +171,14 @@ def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines
             if capacity > 2**31 - 1 or ck_capacity > 2**31 - 1:
                 raise MemoryError("too many (line, tile) pairs or walk checkpoints for one call")
     raise RuntimeError("workspace capacity did not converge")
+
+
+def last_status(dev=None) -> Optional[_native.Status]:
+    """Status of the calling thread's last draw_lines call on the current stream of
+    `dev` (None before the first call): error flags, the render strategy that ran and
+    the pair / checkpoint counts."""
+    dev = torch.device('cuda', torch.cuda.current_device()) if dev is None else torch.device(dev)
+    return _workspace(dev, torch.cuda.current_stream(dev)).last_status
 
 
 def _frames_of(out: torch.Tensor):

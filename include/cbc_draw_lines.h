@@ -69,7 +69,7 @@ typedef struct cbc_tuning {
 /* device-side status, the first bytes of the workspace, read by cbc_read_status */
 typedef struct cbc_status {
     int32_t flags;         /* bit (1 << CBC_ERR_x) for every error seen               */
-    int32_t reserved;
+    int32_t strategy;      /* CBC_STRATEGY_TILES or _LINES: the render the call ran   */
     int64_t bad_line;      /* smallest offending line index (INT64_MAX if none)       */
     int64_t idx_min;       /* smallest frame index in idxs (INT64_MAX if none)        */
     int64_t idx_max;       /* largest frame index in idxs (INT64_MIN if none)         */
@@ -203,11 +203,13 @@ CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *str
  * recorded on each call's stream around its kernels (no effect on results). */
 typedef struct cbc_profile {
     int32_t calls;         /* calls measured since the last reset                    */
-    int32_t reserved;
-    double ms_prep;        /* status init + line records + tile counts               */
-    double ms_offsets;     /* bin offsets                                            */
-    double ms_fill;        /* (line, tile) pair fill                                 */
-    double ms_render;      /* tile render (the dominant kernel)                      */
+    int32_t launches;      /* kernels the library launched since the last reset, in
+                              all calls (forward and backward, profiled or not)     */
+    double ms_prep;        /* status init + line records + tile counts (tiles), or
+                              status init + line records + walk checkpoints (lines) */
+    double ms_offsets;     /* bin offsets (tiles; 0 for lines)                       */
+    double ms_fill;        /* (line, tile) pair fill (tiles; 0 for lines)            */
+    double ms_render;      /* render_kernel (tiles) or segments_kernel (lines)       */
 } cbc_profile;
 
 /* Turn the per-stage event timing on (1) or off (0); returns the previous state. */
