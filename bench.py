@@ -44,8 +44,10 @@ def parse():
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     p.add_argument('--frames', type=int, default=64)
-    p.add_argument('--cpu-frames', type=int, default=8,
-                   help='frames in the bounded CPU-baseline sample')
+    p.add_argument('--cpu-frames', type=int, default=0,
+                   help='frames in the CPU-baseline sample (0: the whole stack); the '
+                        'reference arm sizes its per-step sample to finish in about a '
+                        'minute unless this is set')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--workload', default='detector_stack',
@@ -157,7 +159,8 @@ def cpu_baseline(ls, n_frames: int, repeats: int = 3):
     """The oracle (reference CPU algorithm, C port) on the first frames, all threads."""
     import oracle
     from cbclib_v2_gb300 import workloads
-    sub = workloads.frames_subset(ls, list(range(min(n_frames, ls.shape[0]))))
+    n_frames = ls.shape[0] if n_frames <= 0 else min(n_frames, ls.shape[0])
+    sub = workloads.frames_subset(ls, list(range(n_frames)))
     lines = sub.lines.astype(np.float32)
     threads = len(os.sched_getaffinity(0))
     best = float('inf')
@@ -167,7 +170,7 @@ def cpu_baseline(ls, n_frames: int, repeats: int = 3):
         oracle.draw_lines(out, lines, sub.idxs, sub.max_val, sub.kernel, sub.overlap, threads)
         best = min(best, time.perf_counter() - t0)
     return {'value': sub.n_lines / best / 1e6, 'unit': 'Mlines/s', 'cores': threads,
-            'kind': 'port', 'seconds': best,
+            'kind': 'port', 'seconds': best, 'lines': sub.n_lines,
             'sample': f'{sub.shape[0]} of {ls.shape[0]} frames ({sub.n_lines} lines), '
                       f'best of {repeats}'}
 
@@ -177,18 +180,24 @@ def run_reference(args, ls, world, rank):
         return
     import oracle  # noqa: F401  (builds the C port on first use)
     cfg = workload_config(ls)
-    for _ in range(args.warmup):
-        cpu_baseline(ls, 2, repeats=1)
+    frames = args.cpu_frames
+    for _ in range(max(args.warmup, 1)):
+        probe = cpu_baseline(ls, 2, repeats=1)
+    if frames <= 0:
+        # about 60 s of CPU work over all timed steps, at least one frame per step
+        per_frame = probe['seconds'] / 2
+        frames = int(min(ls.shape[0], max(1, round(60.0 / max(args.steps, 1) / per_frame))))
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(ls, args.cpu_frames, repeats=1))
+        vals.append(cpu_baseline(ls, frames, repeats=1))
     secs = sum(v['seconds'] for v in vals)
-    lines = sum(float(v['sample'].split('(')[1].split()[0]) for v in vals)
+    lines = sum(v['lines'] for v in vals)
     value = lines / secs / 1e6
     cb = dict(vals[0])
     cb['value'] = value
-    cb['sample'] = f'{args.cpu_frames} of {ls.shape[0]} frames per step'
+    cb['sample'] = f'the first {frames} of {ls.shape[0]} frames per step'
     cb.pop('seconds', None)
+    cb.pop('lines', None)
     print(json.dumps({
         'impl': 'reference', 'metric': 'draw_lines throughput', 'value': value,
         'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
@@ -454,7 +463,10 @@ def main():
         'gpu_launches': prof.launches, 'e2e': e2e,
     }
     if not args.no_cpu_baseline and world == 1:
-        res['cpu_baseline'] = cpu_baseline(ls, args.cpu_frames)
+        cb = cpu_baseline(ls, args.cpu_frames, repeats=2)
+        cb.pop('seconds', None)
+        cb.pop('lines', None)
+        res['cpu_baseline'] = cb
     print(json.dumps(res), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -31,21 +31,23 @@ namespace cbc {
 /* max overlap: winner[p] = min over lines l with v_l(p) == image[p] > out0[p] */
 template <typename T, int K>
 struct WinnerAct {
+    static constexpr bool kNeedsGeometry = false;
     const T *image;
     const T *out0;       /* NULL: zeros */
     int *winner;
     T max_val;
     int W;
+    const float *gtab;   /* gaussian table (shared-memory copy) */
     __device__ __forceinline__ void item_begin(int) {}
-    __device__ __forceinline__ void item_end(int, const SlotLine<T> &) {}
-    __device__ __forceinline__ void pixel(const SlotParams<T> &, const SlotLine<T> &sl, int,
-                                          int px, int py, T E, T, T) {
+    __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
+                                          T, T) {
         using A = Ar<T>;
-        const long long at = sl.fbase + (long long)py * W + px;
-        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
+        const long long at = S.fbase[slot] + (long long)py * W + px;
+        const T v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
         const T img = image[at];
         const T o = out0 ? out0[at] : T(0);
-        if (v == img && o < img) atomicMin(winner + at, sl.line);
+        if (v == img && o < img) atomicMin(winner + at, S.line[slot]);
     }
 };
 
@@ -64,6 +66,7 @@ __device__ __forceinline__ T kappa_of(T d, T w, T max_val)
 
 template <typename T, int K, int OV>
 struct BackwardAct {
+    static constexpr bool kNeedsGeometry = true;
     const T *grad_out;
     const int *winner;   /* max overlap */
     double *gacc;        /* (N, 5) */
@@ -74,36 +77,39 @@ struct BackwardAct {
         #pragma unroll
         for (int k = 0; k < 5; k++) acc[lane][k] = T(0);
     }
-    __device__ __forceinline__ void item_end(int lane, const SlotLine<T> &sl) {
-        if (sl.line < 0) return;
+    __device__ __forceinline__ void item_end(int lane, const SlotTable<T> &S) {
+        const int line = S.line[lane];
+        if (line < 0) return;
         #pragma unroll
         for (int k = 0; k < 5; k++) {
             const T v = acc[lane][k];
-            if (v != T(0)) atomicAdd(gacc + (size_t)sl.line * 5 + k, (double)v);
+            if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
         }
     }
-    __device__ __forceinline__ void pixel(const SlotParams<T> &, const SlotLine<T> &sl, int slot,
-                                          int px, int py, T, T, T) {
-        const long long at = sl.fbase + (long long)py * W + px;
-        if (OV == CBC_MAX && winner[at] != sl.line) return;
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
+                                          T) {
+        const long long at = S.fbase[slot] + (long long)py * W + px;
+        if (OV == CBC_MAX && winner[at] != S.line[slot]) return;
         const T g = grad_out[at];
         if (g == T(0)) return;
+        const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
+        const T w = S.w[slot];
         const T X = (T)px, Y = (T)py;
-        const T cx = sl.x0 + T(0.5) * sl.t0, cy = sl.y0 + T(0.5) * sl.t1;
-        const T mag = sl.t0 * sl.t0 + sl.t1 * sl.t1;
-        T t = ((X - cx) * sl.t0 + (Y - cy) * sl.t1) / mag;
+        const T cx = x0 + T(0.5) * t0, cy = y0 + T(0.5) * t1;
+        const T mag = t0 * t0 + t1 * t1;
+        T t = ((X - cx) * t0 + (Y - cy) * t1) / mag;
         t = t < T(-0.5) ? T(-0.5) : (t > T(0.5) ? T(0.5) : t);
-        const T dx = cx + t * sl.t0 - X, dy = cy + t * sl.t1 - Y;
+        const T dx = cx + t * t0 - X, dy = cy + t * t1 - Y;
         const T d2 = dx * dx + dy * dy;
         const T d = sqrt(d2);
-        const T G = g * kappa_of<T, K>(d, sl.w, max_val);
+        const T G = g * kappa_of<T, K>(d, w, max_val);
         if (G == T(0)) return;
         const T s = t + T(0.5);
         atomicAdd(&acc[slot][0], G * (T(1) - s) * dx);
         atomicAdd(&acc[slot][1], G * (T(1) - s) * dy);
         atomicAdd(&acc[slot][2], G * s * dx);
         atomicAdd(&acc[slot][3], G * s * dy);
-        atomicAdd(&acc[slot][4], -G * d2 / sl.w);
+        atomicAdd(&acc[slot][4], -G * d2 / w);
     }
 };
 
@@ -128,6 +134,7 @@ winner_kernel(AdjArgs<T> a)
     act.winner = a.winner;
     act.max_val = a.max_val;
     act.W = a.d.W;
+    act.gtab = stage_gauss_table<T, K>();
     drive_segments(a.d, act);
 }
 
@@ -171,18 +178,23 @@ AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes,
 }
 
 template <typename T, int K>
-cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, int grid, cudaStream_t s)
+cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, cudaStream_t s)
 {
     if (overlap == CBC_MAX) {
+        const unsigned grid = resident_grid(winner_kernel<T, K>, kSegWarps * 32);
         winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
         note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
         if (e != cudaSuccess) return e;
-        backward_kernel<T, K, CBC_MAX><<<grid, kSegWarps * 32, 0, s>>>(aa);
+        backward_kernel<T, K, CBC_MAX><<<resident_grid(backward_kernel<T, K, CBC_MAX>,
+                                                       kSegWarps * 32),
+                                         kSegWarps * 32, 0, s>>>(aa);
     } else {
-        backward_kernel<T, K, CBC_SUM><<<grid, kSegWarps * 32, 0, s>>>(aa);
+        backward_kernel<T, K, CBC_SUM><<<resident_grid(backward_kernel<T, K, CBC_SUM>,
+                                                       kSegWarps * 32),
+                                         kSegWarps * 32, 0, s>>>(aa);
     }
     note_launches(1);
     return cudaGetLastError();
@@ -266,16 +278,12 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.winner = winner;
         aa.gacc = gacc;
         aa.max_val = max_val;
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int grid = sms > 0 ? sms * 8 : 1024;
         switch (kernel) {
-        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, grid, s); break;
-        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, grid, s); break;
-        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, grid, s); break;
-        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, grid, s); break;
-        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, grid, s); break;
+        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, s); break;
+        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, s); break;
+        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, s); break;
+        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, s); break;
+        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, s); break;
         }
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     }

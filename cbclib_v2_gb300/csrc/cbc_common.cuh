@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <limits.h>
+#include <atomic>
 #include <string>
 
 #include "cbc_draw_lines.h"
@@ -117,8 +118,18 @@ template <> struct Ar<float> {
         return p.fast ? cbc_pixel_error_r(te, nf, p.len, p.len2, p.ww, p.rlen, p.rww)
                       : cbc_pixel_error(te, nf, p.len, p.len2, p.ww);
     }
+    /* error() where 0 <= te <= len^2 (no tangent term): the correctly rounded nf / ww */
+    static __device__ __forceinline__ float error_inside(float nf, const SlotParams<float> &p) {
+        return p.fast ? cbc_div(nf, p.ww, p.rww) : cbc_div_ieee(nf, p.ww);
+    }
     template <int K>
     static __device__ __forceinline__ float profile(float x) { return cbc_profile_f32(K, x); }
+    /* the same, the gaussian reading its table from `tab` (null: the global table) */
+    template <int K>
+    static __device__ __forceinline__ float profile_tab(float x, const float *tab) {
+        if (K == CBC_GAUSSIAN && tab) return cbc_gaussian_tab(x, tab);
+        return cbc_profile_f32(K, x);
+    }
     static __device__ __forceinline__ bool fast_range(float v) {
         return v >= CBC_DIV_LO && v <= CBC_DIV_HI;
     }
@@ -146,8 +157,15 @@ template <> struct Ar<double> {
         double a = __ddiv_rn(ta, p.len);
         return __ddiv_rn(__dadd_rn(__dmul_rn(a, a), nf), p.ww);
     }
+    static __device__ __forceinline__ double error_inside(double nf, const SlotParams<double> &p) {
+        return __ddiv_rn(nf, p.ww);
+    }
     template <int K>
     static __device__ __forceinline__ double profile(double x) { return cbc_profile_f64(K, x); }
+    template <int K>
+    static __device__ __forceinline__ double profile_tab(double x, const float *) {
+        return cbc_profile_f64(K, x);
+    }
     static __device__ __forceinline__ bool fast_range(double) { return false; }
 };
 
@@ -167,6 +185,22 @@ __device__ T span_threshold(T len, T ww);
 template <>
 __device__ inline float span_threshold<float>(float len, float ww)
 {
+    auto reaches = [&](unsigned u) {
+        const float b = __fdiv_rn(__uint_as_float(u), len);
+        return __fmul_rn(b, b) >= ww;
+    };
+    /* the answer lies within a few ulps of sqrt(ww) * len: search there first */
+    const float g = __fmul_rn(__fsqrt_rn(ww), len);
+    unsigned u = __float_as_uint(g);
+    if (g > 0.0f && u < 0x7f000000u) {
+        if (reaches(u)) {
+            for (int i = 0; i < 16; i++, u--)
+                if (u == 0u || !reaches(u - 1u)) return __uint_as_float(u);
+        } else {
+            for (int i = 0; i < 16; i++)
+                if (reaches(++u)) return __uint_as_float(u);
+        }
+    }
     unsigned lo = 0u, hi = 0x7f800000u;              /* f(+inf) = inf >= ww */
     while (lo < hi) {
         unsigned mid = lo + ((hi - lo) >> 1);
@@ -321,19 +355,36 @@ struct Walker {
         d0n = sx > 0 ? r.t1 : -r.t1;
         d1n = sy > 0 ? -r.t0 : r.t0;
     }
-    /* decisions at the current position: (next x, next y) */
-    __device__ __forceinline__ void decide(bool &nx, bool &ny, T &exx) const {
+    /* the normal errors of the three candidate moves from the current position:
+     * x only, y only, both (the last is exx + d1n, as the reference adds it) */
+    struct Next {
+        T exx, eyy, exy;
+        bool nx, ny;
+    };
+    /* decisions at the current position: step x (nx) and / or y (ny) */
+    __device__ __forceinline__ Next decide() const {
         using A = Ar<T>;
-        exx = A::add(ne, d0n);
-        T eyy = A::add(ne, d1n);
-        T exy = A::add(exx, d1n);
-        if (fabs(eyy) < fabs(exx)) { ny = true; nx = fabs(exy) < fabs(eyy); }
-        else                       { nx = true; ny = fabs(exy) < fabs(exx); }
+        Next n;
+        n.exx = A::add(ne, d0n);
+        n.eyy = A::add(ne, d1n);
+        n.exy = A::add(n.exx, d1n);
+        const T axx = fabs(n.exx), ayy = fabs(n.eyy), axy = fabs(n.exy);
+        const bool ylt = ayy < axx;
+        n.nx = !ylt || axy < ayy;
+        n.ny = ylt || axy < axx;
+        return n;
     }
-    __device__ __forceinline__ void step(bool nx, bool ny, T exx) {
+    /* take the move: te gains d0t then d1t, ne becomes the move's candidate; written
+     * as selects so that the ne chain is add, add, compare, select per step */
+    __device__ __forceinline__ void step(const Next &n) {
         using A = Ar<T>;
-        if (nx) { cx += sx; te = A::add(te, d0t); ne = exx; }
-        if (ny) { cy += sy; te = A::add(te, d1t); ne = A::add(ne, d1n); }
+        const T ta = A::add(te, d0t);
+        const T tb = A::add(te, d1t);
+        const T tab = A::add(ta, d1t);
+        te = n.nx ? (n.ny ? tab : ta) : tb;
+        ne = n.nx ? (n.ny ? n.exy : n.exx) : n.eyy;
+        cx += n.nx ? sx : 0;
+        cy += n.ny ? sy : 0;
     }
 };
 
@@ -500,11 +551,14 @@ __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> 
     wk.ne = r.ne0;
     const int nck = (r.ncols + kSeg - 1) / kSeg;
     Checkpoint<T> *ck = cks + r.ck_base;
-    int k = 0;
+    int k = 0, next = 0;            /* next checkpoint: the first walk index >= next */
+    const int x_end = r.x1, y_end = r.y1, c0 = r.c0, sa = cv.sa, ax = cv.a;
     long long guard = 0;
-    while (k < nck && wk.cx != r.x1 && wk.cy != r.y1) {
-        const int idx = ((cv.a ? wk.cy : wk.cx) - r.c0) * cv.sa;
-        while (k < nck && idx >= k * kSeg) {
+    /* the walk index starts at or below 0 and grows by at most 1 per step, so a
+     * step passes at most one checkpoint */
+    while (k < nck && wk.cx != x_end && wk.cy != y_end) {
+        const int idx = ((ax ? wk.cy : wk.cx) - c0) * sa;
+        if (idx >= next) {
             Checkpoint<T> c;
             c.cx = wk.cx;
             c.cy = wk.cy;
@@ -513,11 +567,9 @@ __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> 
             c.line = i;
             c.seg = k;
             ck[k++] = c;
+            next += kSeg;
         }
-        bool nx, ny;
-        T exx;
-        wk.decide(nx, ny, exx);
-        wk.step(nx, ny, exx);
+        wk.step(wk.decide());
         if (++guard > 4LL * CBC_MAX_WALK + 64) {
             atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
             break;
@@ -673,24 +725,27 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
 
 /* ---- lines-strategy pixel enumeration ---------------------------------------------
  * Work items are (line, kSeg-column segment) pairs, i.e. walk checkpoints.  A warp
- * takes 32 of them from an atomic counter: every lane resumes its line's walk
- * (bresenham.hpp:352-383 outer loop) from the checkpoint for kSeg columns into the
- * warp's shared entries; the warp then flattens the spans of those entries into one
- * pixel per lane (warp scan + shuffle binary search) and calls
- *     act.pixel(p, line, slot, x, y, E, te, ne)
- * for every pixel the reference draws (visited by the walk, error E <= 1, inside the
- * frame), with act.item_begin(lane) / act.item_end(lane) around each warp item.  The
- * forward, the max-overlap winner pass and the adjoint are such actions. */
+ * takes 32 of them from an atomic counter, one per lane, resumes every lane's walk
+ * (bresenham.hpp:352-383 outer loop) from its checkpoint and handles the segment's
+ * columns in kSeg rounds, one column per lane and round:
+ *   spans:   level k = 0, 1, 2, ... of all 32 columns at once: every lane advances
+ *            the two span walks of its column (the inner loops, :369-380) by one step
+ *            with the reference's float increments, and the visited in-frame pixels
+ *            of the level go into per-warp rings in shared memory (ballot +
+ *            popcount give the positions);
+ *   pixels:  whenever a ring holds 32 pixels, every lane takes one, evaluates the
+ *            error E with the reference's rounding and, for E <= 1, calls
+ *                act.pixel(slots, slot, x, y, E, te, ne).
+ * A span walk ends at its first step with |ne| >= threshold (the reference's loop
+ * condition) or when it leaves the frame.  The walks stay sequential per lane, as in
+ * the reference, while the expensive per-pixel work runs on full warps.
+ * act.item_begin(lane) / act.item_end(lane, slots) bracket each warp item; an action
+ * that reads the line geometry from the slot table sets kNeedsGeometry.  The forward,
+ * the max-overlap winner pass and the adjoint are such actions. */
 
 constexpr int kSegWarps = 4;
-
-/* what an action may need about the line of a slot */
-template <typename T>
-struct SlotLine {
-    long long fbase;    /* frame * H * W                        */
-    int line;           /* line index, -1 for an empty slot     */
-    T x0, y0, t0, t1, w;
-};
+constexpr int kSegMinBlocks = 6;   /* resident CTAs per SM the register budget targets */
+constexpr int kRing = 128;         /* slots per ring, a power of two >= 31 + 64 */
 
 template <typename T>
 struct DriveArgs {
@@ -701,19 +756,124 @@ struct DriveArgs {
     unsigned long long *work;      /* work-item counter, zeroed before the launch */
 };
 
+/* what the error evaluation reads per slot: one 16-byte load for float */
+template <typename T>
+struct alignas(16) EvalSlot {
+    T len, rlen, ww, rww;
+};
+
+/* per-slot (lane) data of a warp's current items, one array per field so that 32
+ * lanes reading 32 different slots hit distinct shared-memory banks */
+template <typename T>
+struct SlotTable {
+    EvalSlot<T> ev[32];
+    T len2[32];
+    int fast[32];        /* len and ww in the range of the reciprocal division */
+    long long fbase[32]; /* frame * H * W                                      */
+    int line[32];        /* line index, -1 for an empty slot                   */
+    T x0[32], y0[32], t0[32], t1[32], w[32];
+};
+
+/* a visited pixel waiting for evaluation: walk errors and frame coordinates, one
+ * 16-byte shared-memory access for float */
+template <typename T>
+struct alignas(16) RingPixel {
+    T te, ne;
+    int x, y;
+};
+
+template <typename T>
+struct PixelRing {
+    RingPixel<T> px[kRing];
+    unsigned char slot[kRing];     /* owner lane of each pixel */
+};
+
 template <typename T, class Act>
 __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
 {
     using A = Ar<T>;
-    __shared__ Entry<T> ent_s[kSegWarps][32 * kSeg];
-    __shared__ SlotParams<T> prm_s[kSegWarps][32];
-    __shared__ SlotLine<T> sln_s[kSegWarps][32];
+    __shared__ SlotTable<T> slot_s[kSegWarps];
+    __shared__ PixelRing<T> ring_s[kSegWarps][2];
     if (a.st->flags & kFatal) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    Entry<T> *ent = ent_s[warp];
-    SlotParams<T> *prm = prm_s[warp];
-    SlotLine<T> *sln = sln_s[warp];
+    SlotTable<T> &S = slot_s[warp];
+    PixelRing<T> *rg = ring_s[warp];
     const long long total = (long long)a.st->cks;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    /* ring cursors, equal in every lane: ring 0 holds pixels within the segment's
+     * extent along the line (0 <= te <= len^2, where the error is the normal term
+     * alone), ring 1 the end-cap pixels, whose error takes the longer exact path;
+     * separate rings keep every evaluation round on one path */
+    unsigned head0 = 0, tail0 = 0, head1 = 0, tail1 = 0;
+
+    auto store = [&](bool cap, unsigned q, T te, T ne, int x, int y) {
+        PixelRing<T> &R = rg[cap ? 1 : 0];
+        RingPixel<T> v;
+        v.te = te;
+        v.ne = ne;
+        v.x = x;
+        v.y = y;
+        R.px[q & (kRing - 1)] = v;
+        R.slot[q & (kRing - 1)] = (unsigned char)lane;
+    };
+    /* append the lanes' pixels with `take` set */
+    auto push = [&](bool take, bool cap, T te, T ne, int x, int y) {
+        const unsigned m1 = __ballot_sync(0xffffffffu, take && cap);
+        const unsigned m0 = __ballot_sync(0xffffffffu, take && !cap);
+        if (take)
+            store(cap, cap ? tail1 + __popc(m1 & lanes_below) : tail0 + __popc(m0 & lanes_below),
+                  te, ne, x, y);
+        tail0 += __popc(m0);
+        tail1 += __popc(m1);
+    };
+    /* the same for two pixels per lane: all (a) pixels precede all (b) pixels */
+    auto push2 = [&](bool ta, bool ca, T tea, T nea, int xa, int ya,
+                     bool tb, bool cb, T teb, T neb, int xb, int yb) {
+        const unsigned a1 = __ballot_sync(0xffffffffu, ta && ca);
+        const unsigned a0 = __ballot_sync(0xffffffffu, ta && !ca);
+        const unsigned b1 = __ballot_sync(0xffffffffu, tb && cb);
+        const unsigned b0 = __ballot_sync(0xffffffffu, tb && !cb);
+        const unsigned na1 = __popc(a1), na0 = __popc(a0);
+        if (ta)
+            store(ca, ca ? tail1 + __popc(a1 & lanes_below) : tail0 + __popc(a0 & lanes_below),
+                  tea, nea, xa, ya);
+        if (tb)
+            store(cb, cb ? tail1 + na1 + __popc(b1 & lanes_below)
+                         : tail0 + na0 + __popc(b0 & lanes_below),
+                  teb, neb, xb, yb);
+        tail0 += na0 + __popc(b0);
+        tail1 += na1 + __popc(b1);
+    };
+    /* evaluate ring pixels, 32 at a time, until at most `keep` remain in the ring */
+    auto drain_ring = [&](PixelRing<T> &R, unsigned &head, unsigned tail, unsigned keep,
+                          bool cap) {
+        while (tail - head > keep) {
+            __syncwarp();
+            const unsigned n = min(tail - head, 32u);
+            if ((unsigned)lane < n) {
+                const unsigned q = (head + lane) & (kRing - 1);
+                const int slot = R.slot[q];
+                const RingPixel<T> v = R.px[q];
+                const EvalSlot<T> ev = S.ev[slot];
+                SlotParams<T> p;
+                p.len = ev.len;
+                p.rlen = ev.rlen;
+                p.ww = ev.ww;
+                p.rww = ev.rww;
+                p.fast = S.fast[slot];
+                if (cap) p.len2 = S.len2[slot];
+                const T nf = A::nterm(v.ne, p);
+                const T E = cap ? A::error(v.te, nf, p) : A::error_inside(nf, p);
+                if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne);
+            }
+            head += n;
+            __syncwarp();
+        }
+    };
+    auto drain = [&](unsigned keep) {
+        drain_ring(rg[0], head0, tail0, keep, false);
+        drain_ring(rg[1], head1, tail1, keep, true);
+    };
 
     for (;;) {
         long long base = 0;
@@ -721,133 +881,152 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= total) break;
         const long long item = base + lane;
-        #pragma unroll
-        for (int k = 0; k < kSeg; k++) ent[lane * kSeg + k].c = kInvalidEntry;
-        sln[lane].line = -1;
+        S.line[lane] = -1;
+
+        Walker<T> wk;
+        int x_end = 0, y_end = 0, c0 = 0, sa = 1, lo = 0, hi = -1, ax = 0, s_hi = -1;
+        T ts = T(0), ns = T(0), thr = T(0), len2 = T(0);
+        bool cols = false;             /* columns of this item left to find */
         if (item < total) {
             const Checkpoint<T> ck = a.cks[item];
             if (ck.cx != INT_MIN) {
                 const LineRec<T> r = a.recs[ck.line];
-                const int ax = r.flags & kAxisY;
-                Walker<T> wk;
+                ax = r.flags & kAxisY;
                 wk.init(r);
                 wk.cx = ck.cx;
                 wk.cy = ck.cy;
                 wk.te = ck.te;
                 wk.ne = ck.ne;
-                const int sa = ax ? wk.sy : wk.sx;
-                const int lo = ck.seg * kSeg, hi = min(lo + kSeg - 1, r.ncols - 1);
-                SlotParams<T> p;
-                p.ts = ax ? r.t0 : r.t1;
-                p.ns = ax ? r.t1 : -r.t0;
-                p.len = r.len;
-                p.len2 = r.len2;
-                p.ww = r.ww;
-                p.rlen = r.rlen;
-                p.rww = r.rww;
-                p.ne_thr = r.ne_thr;
-                p.rns = 1.0f / (float)p.ns;
-                p.ss = ax ? wk.sx : wk.sy;
-                p.axis = ax;
-                p.fast = (r.flags & kFastDiv) ? 1 : 0;
-                prm[lane] = p;
-                SlotLine<T> sl;
-                sl.fbase = (long long)r.frame * a.H * a.W;
-                sl.line = ck.line;
-                sl.x0 = r.px;
-                sl.y0 = r.py;
-                sl.t0 = r.t0;
-                sl.t1 = r.t1;
-                sl.w = r.w;
-                sln[lane] = sl;
-                int guard = 0;
-                while (wk.cx != r.x1 && wk.cy != r.y1) {
-                    bool nx, ny;
-                    T exx;
-                    wk.decide(nx, ny, exx);
-                    const int c = ax ? wk.cy : wk.cx;
-                    const int idx = (c - r.c0) * sa;
-                    if (idx > hi) break;
-                    if ((ax ? ny : nx) && idx >= lo) {
-                        Entry<T> en;
-                        en.c = c;
-                        en.sc = ax ? wk.cx : wk.cy;
-                        en.te = wk.te;
-                        en.ne = wk.ne;
-                        ent[lane * kSeg + (idx - lo)] = en;
-                        if (idx == hi) break;
-                    }
-                    wk.step(nx, ny, exx);
-                    if (++guard > 4 * CBC_MAX_WALK + 64) {
-                        atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
-                        break;
-                    }
+                x_end = r.x1;
+                y_end = r.y1;
+                c0 = r.c0;
+                sa = ax ? wk.sy : wk.sx;
+                lo = ck.seg * kSeg;
+                hi = min(lo + kSeg - 1, r.ncols - 1);
+                s_hi = (ax ? a.W : a.H) - 1;
+                ts = ax ? r.t0 : r.t1;
+                ns = ax ? r.t1 : -r.t0;
+                thr = r.ne_thr;
+                len2 = r.len2;
+                EvalSlot<T> ev;
+                ev.len = r.len;
+                ev.rlen = r.rlen;
+                ev.ww = r.ww;
+                ev.rww = r.rww;
+                S.ev[lane] = ev;
+                S.len2[lane] = r.len2;
+                S.fast[lane] = (r.flags & kFastDiv) ? 1 : 0;
+                S.fbase[lane] = (long long)r.frame * a.H * a.W;
+                S.line[lane] = ck.line;
+                if (Act::kNeedsGeometry) {
+                    S.x0[lane] = r.px;
+                    S.y0[lane] = r.py;
+                    S.t0[lane] = r.t0;
+                    S.t1[lane] = r.t1;
+                    S.w[lane] = r.w;
                 }
+                cols = true;
             }
         }
         act.item_begin(lane);
         __syncwarp();
+
+        int guard = 0;
         #pragma unroll 1
-        for (int b = 0; b < kSeg; b++) {
-            const int e = b * 32 + lane;
-            int cnt = 0, jlo = 0;
-            {
-                const Entry<T> en = ent[e];
-                if (en.c != kInvalidEntry) {
-                    const SlotParams<T> &p = prm[e / kSeg];
-                    cnt = span_window(p, en.sc, en.ne, 0, (p.axis ? a.W : a.H) - 1, jlo);
+        for (int b = 0; b < kSeg && __any_sync(0xffffffffu, cols); b++) {
+            /* this lane's next column: the position of the next long-axis step with
+             * walk index in [lo, hi] */
+            bool col = false;
+            int c = 0, sc = 0;
+            T te_c = T(0), ne_c = T(0);
+            while (cols && wk.cx != x_end && wk.cy != y_end) {
+                const typename Walker<T>::Next mv = wk.decide();
+                const int cc = ax ? wk.cy : wk.cx;
+                const int idx = (cc - c0) * sa;
+                if (idx > hi) break;
+                const bool here = (ax ? mv.ny : mv.nx) && idx >= lo;
+                if (here) {
+                    col = true;
+                    c = cc;
+                    sc = ax ? wk.cx : wk.cy;
+                    te_c = wk.te;
+                    ne_c = wk.ne;
+                    if (idx == hi) cols = false;
                 }
+                wk.step(mv);
+                if (++guard > 4 * CBC_MAX_WALK + 64) {
+                    atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                    col = false;
+                    break;
+                }
+                if (here) break;
             }
-            int incl = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-                int u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += u;
-            }
-            const int excl = incl - cnt;
-            const int items = __shfl_sync(0xffffffffu, incl, 31);
-            for (int t0 = 0; t0 < items; t0 += 32) {
-                const int t = t0 + lane;
-                int o = 0;
-                #pragma unroll
-                for (int bit = 16; bit > 0; bit >>= 1) {
-                    const int v = __shfl_sync(0xffffffffu, excl, o + bit);
-                    if (v <= t) o += bit;
-                }
-                const int off_o = __shfl_sync(0xffffffffu, excl, o);
-                const int jlo_o = __shfl_sync(0xffffffffu, jlo, o);
-                if (t >= items) continue;
-                const int eo = b * 32 + o;
-                const int slot = eo / kSeg;
-                const Entry<T> en = ent[eo];
-                const SlotParams<T> &p = prm[slot];
-                const int j = jlo_o + (t - off_o);
-                T te = en.te, ne = en.ne;
-                bool visited = true;
-                if (j != 0) {
-                    const T dt = j > 0 ? p.ts : -p.ts, dn = j > 0 ? p.ns : -p.ns;
-                    te = A::add(te, dt);
-                    ne = A::add(ne, dn);
-                    visited = fabs(ne) < p.ne_thr;
-                    const int k = j > 0 ? j : -j;
-                    for (int q = 1; q < k; q++) {
-                        te = A::add(te, dt);
-                        ne = A::add(ne, dn);
-                    }
-                    visited = visited && fabs(ne) < p.ne_thr;
-                }
-                if (!visited) continue;
-                const T nf = A::nterm(ne, p);
-                const T E = A::error(te, nf, p);
-                if (!(E <= T(1))) continue;
-                const int y = en.sc + j;
-                const int px = p.axis ? y : en.c, py = p.axis ? en.c : y;
-                act.pixel(p, sln[slot], slot, px, py, E, te, ne);
+            if (!col) cols = false;
+
+            /* level 0: the column's centre pixel */
+            push(col && sc >= 0 && sc <= s_hi, te_c < T(0) || te_c > len2, te_c, ne_c,
+                 ax ? sc : c, ax ? c : sc);
+            drain(31);
+            /* levels 1, 2, ...: one step of the upward and the downward span walk */
+            T tu = te_c, nu = ne_c, td = te_c, nd = ne_c;
+            bool up = col, dn = col;
+            for (int k = 1;; k++) {
+                /* both walks step every level; a finished walk's values go unused */
+                tu = A::add(tu, ts);
+                nu = A::add(nu, ns);
+                td = A::sub(td, ts);
+                nd = A::sub(nd, ns);
+                const int su = sc + k, sd = sc - k;
+                up = up && fabs(nu) < thr && su <= s_hi;
+                dn = dn && fabs(nd) < thr && sd >= 0;
+                if (!__any_sync(0xffffffffu, up || dn)) break;
+                push2(up && su >= 0, tu < T(0) || tu > len2, tu, nu, ax ? su : c, ax ? c : su,
+                      dn && sd <= s_hi, td < T(0) || td > len2, td, nd, ax ? sd : c, ax ? c : sd);
+                drain(31);
             }
         }
+        drain(0);
         __syncwarp();
-        act.item_end(lane, sln[lane]);
+        act.item_end(lane, S);
         __syncwarp();
     }
+}
+
+/* the float gaussian's table copied into shared memory at kernel start (random
+ * per-lane entries: a shared-memory gather instead of one L1 sector per lane);
+ * null for the other profiles and for double.  Every thread of the CTA calls it. */
+template <typename T, int K>
+__device__ __forceinline__ const float *stage_gauss_table()
+{
+    if constexpr (K == CBC_GAUSSIAN && sizeof(T) == sizeof(float)) {
+        __shared__ float2 tab[CBC_EXP_TABLE_N];
+        const float2 *src = reinterpret_cast<const float2 *>(&cbc_gauss_table[0][0]);
+        for (int i = threadIdx.x; i < CBC_EXP_TABLE_N; i += blockDim.x) tab[i] = src[i];
+        __syncthreads();
+        return reinterpret_cast<const float *>(tab);
+    } else {
+        return nullptr;
+    }
+}
+
+/* grid of a persistent kernel: the CTAs of `threads` threads that are resident at
+ * once on the current device (cached per kernel and device) */
+template <typename F>
+unsigned resident_grid(F kernel, int threads)
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::atomic<int> &c = cache[dev & 63];
+    int g = c.load(std::memory_order_relaxed);
+    if (g == 0) {
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+        g = (sms > 0 ? sms : 132) * (per_sm > 0 ? per_sm : 1);
+        c.store(g, std::memory_order_relaxed);
+    }
+    return (unsigned)g;
 }
 
 /* host-side error reporting, defined in cbc_draw_lines.cu */

@@ -184,12 +184,10 @@ render_kernel(RenderArgs<T> a)
             wk.ne = ck.ne;
             int guard = 0;
             while (wk.cx != w.x1 && wk.cy != w.y1) {
-                bool nx, ny;
-                T exx;
-                wk.decide(nx, ny, exx);
+                const typename Walker<T>::Next mv = wk.decide();
                 const int c = w.axis ? wk.cy : wk.cx;
                 const int idx = (c - w.c0) * w.sa;
-                if (w.axis ? ny : nx) {
+                if (w.axis ? mv.ny : mv.nx) {
                     if (idx >= lo && idx <= hi) {
                         const int k = w.ent_base + (idx - w.k_lo);
                         Entry<T> en;
@@ -203,7 +201,7 @@ render_kernel(RenderArgs<T> a)
                     }
                 }
                 if (idx > hi) break;
-                wk.step(nx, ny, exx);
+                wk.step(mv);
                 if (++guard > 4 * CBC_MAX_WALK + 64) {
                     atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
                     break;
@@ -311,16 +309,18 @@ render_kernel(RenderArgs<T> a)
 
 template <typename T, int K, int OV>
 struct ForwardAct {
+    static constexpr bool kNeedsGeometry = false;
     T *out;
     T max_val;
     int W;
+    const float *gtab;   /* gaussian table (shared-memory copy) */
     __device__ __forceinline__ void item_begin(int) {}
-    __device__ __forceinline__ void item_end(int, const SlotLine<T> &) {}
-    __device__ __forceinline__ void pixel(const SlotParams<T> &, const SlotLine<T> &sl, int,
-                                          int px, int py, T E, T, T) {
+    __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
+                                          T, T) {
         using A = Ar<T>;
-        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
-        T *dst = out + sl.fbase + (long long)py * W + px;
+        const T v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
+        T *dst = out + S.fbase[slot] + (long long)py * W + px;
         if (OV == CBC_SUM) atomicAdd(dst, v); else global_combine_max(dst, v);
     }
 };
@@ -333,13 +333,14 @@ struct SegArgs {
 };
 
 template <typename T, int K, int OV>
-__global__ void __launch_bounds__(kSegWarps * 32)
+__global__ void __launch_bounds__(kSegWarps * 32, kSegMinBlocks)
 segments_kernel(SegArgs<T> a)
 {
     ForwardAct<T, K, OV> act;
     act.out = a.out;
     act.max_val = a.max_val;
     act.W = a.d.W;
+    act.gtab = stage_gauss_table<T, K>();
     drive_segments(a.d, act);
 }
 
@@ -496,10 +497,9 @@ cudaError_t launch_render_k(const RenderArgs<T> &ra, int kernel, int overlap, lo
 template <typename T, int K, int OV>
 cudaError_t launch_segments(const SegArgs<T> &sa, cudaStream_t s)
 {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    segments_kernel<T, K, OV><<<(unsigned)(sms > 0 ? sms * 9 : 1024), kSegWarps * 32, 0, s>>>(sa);
+    /* persistent grid: every CTA that fits at once, no more */
+    const unsigned grid = resident_grid(segments_kernel<T, K, OV>, kSegWarps * 32);
+    segments_kernel<T, K, OV><<<grid, kSegWarps * 32, 0, s>>>(sa);
     note_launches(1);
     return cudaGetLastError();
 }

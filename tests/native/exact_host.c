@@ -2,7 +2,16 @@
  * tests can compare it with the oracle on the CPU.  Built with -ffp-contract=off. */
 #include <stdint.h>
 static long long cbc_slow_count = 0;
+#define CBC_SLOW_HOOK() (cbc_slow_count++)
 #include "exact.cuh"
+
+/* evaluations that left the float pair path since the last call */
+long long exact_take_slow_count(void)
+{
+    long long c = cbc_slow_count;
+    cbc_slow_count = 0;
+    return c;
+}
 
 void exact_profile_batch(int kernel, const float *x, float *out, int64_t n)
 {

@@ -26,6 +26,7 @@ def exact(tmp_path_factory):
     lib.exact_pixel_error_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_pixel_error_r_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_div_batch.argtypes = [P] * 3 + [ctypes.c_int64]
+    lib.exact_take_slow_count.restype = ctypes.c_longlong
     return lib
 
 
@@ -105,3 +106,28 @@ def test_reciprocal_division(exact):
     want = a / b
     same = (got == want) | (np.isnan(got) & np.isnan(want))
     assert same.all()
+
+
+@pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'parabolic'])
+def test_profiles_rarely_leave_fast_path(exact, kernel):
+    """the float pair path decides all but a tiny fraction of random inputs (the double
+    fallback is for near-ties only)"""
+    rng = np.random.default_rng(5)
+    x = np.ascontiguousarray(rng.random(1_000_000, dtype=np.float32))
+    out = np.empty_like(x)
+    exact.exact_take_slow_count()
+    exact.exact_profile_batch(oracle.KERNELS[kernel], _p(x), _p(out), x.size)
+    assert exact.exact_take_slow_count() < 1000     # under 0.1 %
+
+
+def test_pixel_error_rarely_leaves_fast_path(exact):
+    rng = np.random.default_rng(6)
+    m = 1_000_000
+    ln = (rng.random(m) * 100 + 1).astype(np.float32)
+    w = (rng.random(m) * 6 + 0.5).astype(np.float32)
+    te = (ln * ln + (rng.random(m) * 2 - 1) * w * ln).astype(np.float32)   # end caps
+    ne = ((rng.random(m) * 2 - 1) * w * ln).astype(np.float32)
+    out = np.empty_like(te)
+    exact.exact_take_slow_count()
+    exact.exact_pixel_error_r_batch(_p(te), _p(ne), _p(ln), _p(w), _p(out), m)
+    assert exact.exact_take_slow_count() < 1000     # under 0.1 %
