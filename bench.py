@@ -51,12 +51,16 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--workload', default='detector_stack',
-                   choices=['detector_stack', 'fit', 'ragged'],
+                   choices=['detector_stack', 'fit', 'ragged', 'fit_loop'],
                    help='detector_stack: the headline forward; fit: forward + adjoint '
                         'iterations on 8 x 1024^2 frames vs a finite-difference gradient; '
                         'ragged: 256 x 1024^2 frames with lognormal line counts, one '
-                        'CUDA-graph launch vs per-frame plain launches')
-    return p.parse_args()
+                        'CUDA-graph launch vs per-frame plain launches; fit_loop: 100 '
+                        'Adam steps of the streak fit on 32 x 2167x2070 frames, 160k '
+                        'biweight lines, max overlap')
+    args = p.parse_args()
+    args.steps_given = any(a == '--steps' or a.startswith('--steps=') for a in sys.argv[1:])
+    return args
 
 
 def dist_env():
@@ -333,9 +337,54 @@ def run_ragged(args, world, rank, local):
             'graph_speedup_vs_per_frame': ms_frames / ms_graph}), flush=True)
 
 
+def run_fit_loop(args, world, rank, local):
+    """the streak-fit loop: 32 frames of 2167x2070, 5,000 biweight lines per frame,
+    max overlap; the target is the render of the true lines, the start is the truth
+    perturbed by N(0, 1 px) on the endpoints and N(0, 0.3 px) on the widths; 100 Adam
+    steps of lr 0.05 (--steps overrides the count); reports steps/s and the parameter
+    RMS against the truth before and after"""
+    import torch
+    from cbclib_v2_gb300 import draw_lines, fit, workloads
+    torch.cuda.set_device(local)
+    ls = workloads.fit_loop_stack(seed=4000 + rank)
+    dev = torch.device('cuda', local)
+    truth = torch.from_numpy(ls.lines.astype(np.float32)).to(dev)
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)
+    target = torch.zeros(ls.shape, device=dev)
+    draw_lines(target, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
+    start = torch.from_numpy(workloads.perturbed(ls.lines, 4100 + rank, 1.0, 0.3)
+                             .astype(np.float32)).to(dev)
+    steps = args.steps if args.steps_given else 100
+    fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel,
+                  overlap=ls.overlap, steps=max(args.warmup, 1), lr=0.05)      # warm-up
+    res = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel,
+                        overlap=ls.overlap, steps=steps, lr=0.05)
+
+    def rms(p):
+        d = (p - truth).double()
+        return {'endpoints_px': float(d[:, :4].pow(2).mean().sqrt()),
+                'width_px': float(d[:, 4].pow(2).mean().sqrt())}
+
+    if rank == 0:
+        print(json.dumps({
+            'metric': 'streak-fit Adam steps/s', 'value': world * 1e3 / res.ms_per_step,
+            'unit': 'steps/s', 'n_gpus': world, 'steps': steps, 'warmup': args.warmup,
+            'ms_per_step': res.ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+                       'kernel': ls.kernel, 'overlap': ls.overlap, 'lr': 0.05,
+                       'loss': 'sum((I - T)^2), T = render of the true lines (no noise)',
+                       'start': 'truth + N(0, 1 px) endpoints, N(0, 0.3 px) widths'},
+            'rms_start': rms(start), 'rms_final': rms(res.lines),
+            'loss_start': res.losses[0], 'loss_final': res.losses[-1]}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
+    if args.workload == 'fit_loop' and args.impl == 'gb300':
+        run_fit_loop(args, world, rank, local)
+        return
     if args.workload == 'fit' and args.impl == 'gb300':
         run_fit(args, world, rank, local)
         return

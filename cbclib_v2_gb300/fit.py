@@ -1,0 +1,64 @@
+"""Least-squares refinement of line parameters against measured frames with Adam,
+through the differentiable draw_lines (forward and adjoint kernels).
+
+This is the loop that follows ``Streaks.pattern_image`` in the reference's workflow
+(cbclib_v2/_src/streaks.py:65-131): the lines of detected streaks, drawn with a
+profile, are moved so that the drawn frames match the measured ones.  The loss is
+sum((draw(lines) - target)^2) over all frames; the widths are kept at or above
+``min_width`` after every step (a line of width <= 0 draws nothing and gets no
+gradient).
+"""
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import torch
+
+from .autograd import draw_lines_fn
+
+__all__ = ['FitResult', 'fit_lines']
+
+
+@dataclass
+class FitResult:
+    lines: torch.Tensor                  # (N, 5) fitted parameters
+    steps: int
+    seconds: float                       # wall time of the steps (synchronised)
+    losses: List[float] = field(default_factory=list)   # loss before step 0 and after the last
+
+    @property
+    def ms_per_step(self) -> float:
+        return 1e3 * self.seconds / max(self.steps, 1)
+
+
+def _loss(params, idxs, target, max_val, kernel, overlap):
+    img = draw_lines_fn(params, idxs, shape=target.shape, max_val=max_val, kernel=kernel,
+                        overlap=overlap)
+    return ((img - target) ** 2).sum()
+
+
+def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.Tensor] = None,
+              *, max_val: float = 1.0, kernel: str = 'biweight', overlap: str = 'sum',
+              steps: int = 100, lr: float = 0.05, min_width: float = 0.5) -> FitResult:
+    """Refine ``lines0`` (N, 5) so that draw_lines(lines) matches ``target`` (frames on
+    the GPU), with ``steps`` Adam steps of learning rate ``lr``."""
+    if not target.is_cuda:
+        raise ValueError("target must be a CUDA tensor")
+    params = lines0.detach().to(target.device, target.dtype).clone().requires_grad_(True)
+    opt = torch.optim.Adam([params], lr=lr)
+    with torch.no_grad():
+        first = float(_loss(params, idxs, target, max_val, kernel, overlap))
+    torch.cuda.synchronize(target.device)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        loss = _loss(params, idxs, target, max_val, kernel, overlap)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            params[:, 4].clamp_(min=min_width)
+    torch.cuda.synchronize(target.device)
+    seconds = time.perf_counter() - t0
+    with torch.no_grad():
+        last = float(_loss(params, idxs, target, max_val, kernel, overlap))
+    return FitResult(params.detach(), steps, seconds, [first, last])

@@ -95,6 +95,20 @@ def fit_stack(seed: int = 0, F: int = 8, H: int = 1024, W: int = 1024,
                    max_val=100.0 / 0.9375)
 
 
+def fit_loop_stack(seed: int = 0, F: int = 32, H: int = 2167, W: int = 2070,
+                   per_frame: int = 5000) -> LineSet:
+    """32 detector frames of 2167x2070 with 5,000 segments each, distributed as in the
+    single-frame workload; biweight profile, max overlap, a single line's peak at 100
+    counts.  The streak-fit loop starts from these lines perturbed by N(0, 1 px) on
+    the endpoints and N(0, 0.3 px) on the widths."""
+    rng = np.random.default_rng(seed)
+    n = F * per_frame
+    lines = _segments(rng, n, H, W, rng.uniform(10, 100, n), rng.uniform(1, 5, n))
+    idxs = np.repeat(np.arange(F, dtype=np.int64), per_frame)
+    return LineSet(f'fit_loop_stack_{F}x{H}x{W}', (F, H, W), lines, idxs, 'biweight', 'max',
+                   max_val=100.0 / 0.9375)
+
+
 def perturbed(lines: np.ndarray, seed: int, sigma_pt: float = 0.5,
               sigma_w: float = 0.2) -> np.ndarray:
     """lines with endpoints moved by N(0, sigma_pt) and widths by N(0, sigma_w)"""
