@@ -10,10 +10,11 @@ Prints one JSON line (rank 0).  `value` is device-resident throughput in Mlines/
 public API with pinned host buffers (frames, lines and indices copied in, frames
 copied out every step).  `roofline` is the dominant kernel's achieved HBM bandwidth
 (segments_kernel or render_kernel, whichever strategy the call ran) from CUDA events
-recorded on its stream around every launch in the timed region; its byte count is a
-read and a write of every 32-byte sector of the output that holds a drawn pixel plus
-24 bytes per line (the full-frame read-modify-write, 2*F*H*W*4 + N*24, is reported
-beside it as `full_frame_rmw_frac`).  `gpu_launches` is the library's own count of
+recorded on its stream around every launch in the timed region.  Its byte count is the
+call's contract: draw_lines updates `out` in place, so every output pixel is read and
+written once, plus 24 bytes per line (2*F*H*W*4 + 24*N); `write_once_frac` is the same
+for an output known to be zero, and `sparse_model` counts only the 32-byte sectors that
+hold a drawn pixel (the kernel never touches the others).  `gpu_launches` is the library's own count of
 the kernels it launched in the timed region.  `cpu_baseline`
 times the oracle (C port of the reference CPU rasteriser) on a bounded sample with
 all host threads.  Under torchrun each rank renders its own stack (weak scaling, no
@@ -339,7 +340,8 @@ def run_ragged(args, world, rank, local):
 
 def run_fit_loop(args, world, rank, local):
     """the streak-fit loop: 32 frames of 2167x2070, 5,000 biweight lines per frame,
-    max overlap; the target is the render of the true lines, the start is the truth
+    max overlap; the target is Poisson noise on the render of the true lines (peak 100
+    counts), the start is the truth
     perturbed by N(0, 1 px) on the endpoints and N(0, 0.3 px) on the widths; 100 Adam
     steps of lr 0.05 (--steps overrides the count); reports steps/s and the parameter
     RMS against the truth before and after"""
@@ -352,6 +354,8 @@ def run_fit_loop(args, world, rank, local):
     idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)
     target = torch.zeros(ls.shape, device=dev)
     draw_lines(target, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
+    gen = torch.Generator(device=dev).manual_seed(4200 + rank)
+    target = torch.poisson(target, generator=gen)          # counts, peak 100 per line
     start = torch.from_numpy(workloads.perturbed(ls.lines, 4100 + rank, 1.0, 0.3)
                              .astype(np.float32)).to(dev)
     steps = args.steps if args.steps_given else 100
@@ -373,7 +377,8 @@ def run_fit_loop(args, world, rank, local):
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
                        'kernel': ls.kernel, 'overlap': ls.overlap, 'lr': 0.05,
-                       'loss': 'sum((I - T)^2), T = render of the true lines (no noise)',
+                       'loss': 'sum((I - T)^2), T = Poisson(render of the true lines), '
+                               'peak 100 counts',
                        'start': 'truth + N(0, 1 px) endpoints, N(0, 0.3 px) widths'},
             'rms_start': rms(start), 'rms_final': rms(res.lines),
             'loss_start': res.losses[0], 'loss_final': res.losses[-1]}), flush=True)
@@ -489,14 +494,20 @@ def main():
     drawn_sectors = int(out.reshape(-1, 8).ne(0).any(dim=1).sum().item())
     algo_bytes = 64 * drawn_sectors + N * 24
     full_bytes = 2 * F * H * W * 4 + N * 24
-    achieved = algo_bytes / (render_ms * 1e-3) / 1e9
+    achieved = full_bytes / (render_ms * 1e-3) / 1e9
+    sparse = algo_bytes / (render_ms * 1e-3) / 1e9
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_src,
                 'traffic': committed_traffic(ls.name, kname), 'kernel': kname,
-                'algorithmic_bytes': algo_bytes,
-                'bytes_model': 'read+write of each 32 B sector holding a drawn pixel '
-                               '(%d of %d sectors) + 24 B per line' % (drawn_sectors, F * H * W // 8),
-                'full_frame_rmw_frac': full_bytes / (render_ms * 1e-3) / 1e9 / peak,
+                'algorithmic_bytes': full_bytes,
+                'bytes_model': 'read + write of every output pixel (the call updates out '
+                               'in place) + 24 B per line: 2*F*H*W*4 + 24*N',
+                'write_once_frac': (full_bytes / 2 + N * 12) / (render_ms * 1e-3) / 1e9 / peak,
+                'sparse_model': {'bytes': algo_bytes, 'achieved': sparse,
+                                 'frac': sparse / peak,
+                                 'model': 'read+write of each 32 B sector holding a drawn '
+                                          'pixel (%d of %d sectors) + 24 B per line'
+                                          % (drawn_sectors, F * H * W // 8)},
                 'ms_per_launch': render_ms,
                 'stage_ms_per_call': {
                     'prep': prof.ms_prep / max(prof.calls, 1),
