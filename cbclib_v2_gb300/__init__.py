@@ -3,7 +3,7 @@
 module of the reference README.  Compute runs only in the CUDA library built from
 ``csrc/`` (C ABI: include/cbc_draw_lines.h)."""
 from . import device, ndimage
-from .ndimage import draw_lines
+from .ndimage import accumulate_lines, draw_lines
 
 __version__ = '0.1.0'
-__all__ = ['device', 'ndimage', 'draw_lines']
+__all__ = ["device", "ndimage", "draw_lines", "accumulate_lines"]

@@ -11,7 +11,7 @@ CSRC = os.path.join(PKG, 'csrc')
 INCLUDE = os.path.join(ROOT, 'include')
 LIBDIR = os.path.join(PKG, '_lib')
 LIB = os.path.join(LIBDIR, 'libcbc_gb300.so')
-SOURCES = ['cbc_draw_lines.cu', 'cbc_adjoint.cu']
+SOURCES = ['cbc_draw_lines.cu', 'cbc_adjoint.cu', 'cbc_accumulate.cu']
 DEPS = ['exact.cuh', 'exp_table.inc', 'cbc_common.cuh']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

@@ -1,0 +1,417 @@
+/*
+ * cbc_accumulate.cu — accumulate_lines for 2-D lines on sm_103a.
+ *
+ * Reference: accumulate_lines_nd_impl (cbclib_v2/_src/src/bresenham.cpp:151-259) and
+ * its GPU counterpart (cuda_draw_lines.cu:467-523, :687-767, :948-1057).  Lines carry a
+ * term index, terms a frame index.  Every term is drawn into a zeroed buffer of its own,
+ * combining its lines with `in_overlap` (sum or std::max), and the pixels the term's
+ * walks drew are then merged into out[frame(term)] with `out_overlap`.
+ *
+ * The pixels and their values are the forward's (drive_segments, cbc_common.cuh, over
+ * walk checkpoints from prep_kernel).  The four overlap pairs map to:
+ *   sum, sum  one L2 reduction per pixel: out += v (only the addition order differs
+ *             from the reference's term-by-term sums);
+ *   max, max  out = std::max(out, max(+0, v)): a term buffer starts at zero, so every
+ *             pixel a term draws is merged with at least +0 (bit-exact);
+ *   max, sum  a term's value at a pixel must be complete before it is added: per
+ *   sum, max  (term, pixel) values go into an open-addressing hash table in the
+ *             workspace (key term << 32 | pixel, linear probing, at most 64 probes),
+ *             combined there with atomics, then one pass over the table merges every
+ *             entry into `out`.  A full table sets CBC_ERR_CAPACITY and the call draws
+ *             nothing; pairs_needed then holds a table capacity to retry with.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <limits.h>
+#include <string>
+
+#include "cbc_common.cuh"
+
+namespace cbc {
+
+/* bit 0: terms combine their lines by max; bit 1: terms merge into out by max
+ * (the Update encoding of bresenham.cpp:304-307) */
+enum : int { kAccSumSum = 0, kAccMaxSum = 1, kAccSumMax = 2, kAccMaxMax = 3 };
+
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr int kMaxProbe = 64;
+
+/* splitmix64's finaliser (Steele, Lea and Flood 2014) as the table's hash */
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+/* std::max(buffer, v) with buffer starting at +0, as an atomic on the slot's value */
+template <typename T>
+__device__ __forceinline__ void term_combine_max(T *slot, T v);
+
+template <>
+__device__ __forceinline__ void term_combine_max<float>(float *slot, float v)
+{
+    /* the slot holds +0 or a positive value: only v > 0 can change it, and positive
+     * floats order as their bit patterns (NaN and negative v leave it unchanged) */
+    if (v > 0.0f) atomicMax(reinterpret_cast<int *>(slot), __float_as_int(v));
+}
+
+template <>
+__device__ __forceinline__ void term_combine_max<double>(double *slot, double v)
+{
+    if (v > 0.0) atomicMax(reinterpret_cast<long long *>(slot), __double_as_longlong(v));
+}
+
+template <typename T, int K, int MODE>
+struct AccumAct {
+    static constexpr bool kNeedsGeometry = false;
+    T *out;
+    T max_val;
+    int W;
+    const float *gtab;
+    const int *term_of_line;
+    unsigned long long *keys;
+    T *vals;
+    unsigned long long mask;       /* table capacity - 1 (a power of two) */
+    DevStatus *st;
+    __device__ __forceinline__ void item_begin(int) {}
+    __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
+                                          T, T) {
+        using A = Ar<T>;
+        const T v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
+        const long long pix = (long long)py * W + px;
+        if (MODE == kAccSumSum) {
+            atomicAdd(out + S.fbase[slot] + pix, v);
+        } else if (MODE == kAccMaxMax) {
+            global_combine_max(out + S.fbase[slot] + pix, T(0) < v ? v : T(0));
+        } else {
+            const unsigned long long key =
+                ((unsigned long long)(unsigned)term_of_line[S.line[slot]] << 32) |
+                (unsigned long long)(unsigned)pix;
+            unsigned long long h = mix64(key) & mask;
+            for (int probe = 0; probe < kMaxProbe; probe++) {
+                unsigned long long k = *reinterpret_cast<volatile unsigned long long *>(keys + h);
+                if (k == kEmptyKey) k = atomicCAS(keys + h, kEmptyKey, key);
+                if (k == kEmptyKey || k == key) {
+                    if (MODE & 1) term_combine_max(vals + h, v);
+                    else atomicAdd(vals + h, v);
+                    return;
+                }
+                h = (h + 1) & mask;
+            }
+            atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+            atomicMax(&st->pairs, 4ull * (mask + 1));
+        }
+    }
+};
+
+template <typename T>
+struct AccArgs {
+    DriveArgs<T> d;
+    T *out;
+    T max_val;
+    const int *term_of_line;
+    unsigned long long *keys;
+    T *vals;
+    unsigned long long mask;
+};
+
+template <typename T, int K, int MODE>
+__global__ void __launch_bounds__(kSegWarps * 32, kSegMinBlocks)
+accumulate_kernel(AccArgs<T> a)
+{
+    AccumAct<T, K, MODE> act;
+    act.out = a.out;
+    act.max_val = a.max_val;
+    act.W = a.d.W;
+    act.gtab = stage_gauss_table<T, K>();
+    act.term_of_line = a.term_of_line;
+    act.keys = a.keys;
+    act.vals = a.vals;
+    act.mask = a.mask;
+    act.st = a.d.st;
+    drive_segments(a.d, act);
+}
+
+/* every frames[t] in [0, n_frames) (bresenham.cpp:23-36: "frames range (min, max) is
+ * outside of (0, n_frames)"); the int32 copy feeds the merge */
+template <typename FI>
+__global__ void __launch_bounds__(kThreads)
+frames_check_kernel(const FI *__restrict__ frames, long long n_terms, long long n_frames,
+                    int *__restrict__ frame_of_term, DevStatus *st)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = t < n_terms;
+    const long long f = in ? (long long)frames[t] : 0;
+    warp_minmax(f, in, st);
+    if (!in) return;
+    if (f < 0 || f >= n_frames) atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
+    frame_of_term[t] = (f >= 0 && f < n_frames) ? (int)f : 0;
+}
+
+/* per line: its term (bresenham.cpp:182-188: "Term index t is out of range (0, T)")
+ * and its frame */
+template <typename TI>
+__global__ void __launch_bounds__(kThreads)
+term_frames_kernel(const TI *__restrict__ terms, const int *__restrict__ frame_of_term,
+                   long long n_lines, long long n_terms, int *__restrict__ term_of_line,
+                   int *__restrict__ frame_of_line, DevStatus *st)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    const long long t = (long long)terms[i];
+    if (t < 0 || t >= n_terms) {
+        atomicOr(&st->flags, 1 << CBC_ERR_TERM);
+        atomicMin(&st->bad_line, (unsigned long long)i);
+        term_of_line[i] = 0;
+        frame_of_line[i] = 0;
+        return;
+    }
+    term_of_line[i] = (int)t;
+    frame_of_line[i] = frame_of_term[t];
+}
+
+/* the table's entries merged into out with out_overlap (sum: out = v + out;
+ * max: out = std::max(out, v)); nothing when the call has failed */
+template <typename T, int OUT_MAX>
+__global__ void __launch_bounds__(kThreads)
+merge_kernel(T *__restrict__ out, const unsigned long long *__restrict__ keys,
+             const T *__restrict__ vals, long long cap, const int *__restrict__ frame_of_term,
+             long long frame_px, const DevStatus *st)
+{
+    if (st->flags & kFatal) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[i];
+        if (k == kEmptyKey) continue;
+        const int term = (int)(k >> 32);
+        T *dst = out + (long long)frame_of_term[term] * frame_px + (long long)(k & 0xffffffffull);
+        if (OUT_MAX) global_combine_max(dst, vals[i]);
+        else atomicAdd(dst, vals[i]);
+    }
+}
+
+struct AccLayout {
+    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals, total;
+};
+
+AccLayout acc_layout(long long n_lines, long long n_terms, long long ck_capacity,
+                     long long table_capacity, size_t rec_bytes, size_t ck_bytes, size_t elem)
+{
+    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+    AccLayout L;
+    size_t off = 0;
+    L.status = off;        off = up(off + sizeof(DevStatus));
+    L.recs = off;          off = up(off + rec_bytes * (size_t)n_lines);
+    L.cks = off;           off = up(off + ck_bytes * (size_t)ck_capacity);
+    L.frame_of_line = off; off = up(off + sizeof(int) * (size_t)n_lines);
+    L.term_of_line = off;  off = up(off + sizeof(int) * (size_t)n_lines);
+    L.frame_of_term = off; off = up(off + sizeof(int) * (size_t)n_terms);
+    L.keys = off;          off = up(off + sizeof(unsigned long long) * (size_t)table_capacity);
+    L.vals = off;          off = up(off + elem * (size_t)table_capacity);
+    L.total = off;
+    return L;
+}
+
+template <typename T, int K>
+cudaError_t launch_accumulate(const AccArgs<T> &a, int mode, cudaStream_t s)
+{
+    const unsigned threads = kSegWarps * 32;
+    switch (mode) {
+    case kAccSumSum:
+        accumulate_kernel<T, K, kAccSumSum><<<resident_grid(accumulate_kernel<T, K, kAccSumSum>,
+                                                            threads), threads, 0, s>>>(a);
+        break;
+    case kAccMaxSum:
+        accumulate_kernel<T, K, kAccMaxSum><<<resident_grid(accumulate_kernel<T, K, kAccMaxSum>,
+                                                            threads), threads, 0, s>>>(a);
+        break;
+    case kAccSumMax:
+        accumulate_kernel<T, K, kAccSumMax><<<resident_grid(accumulate_kernel<T, K, kAccSumMax>,
+                                                            threads), threads, 0, s>>>(a);
+        break;
+    default:
+        accumulate_kernel<T, K, kAccMaxMax><<<resident_grid(accumulate_kernel<T, K, kAccMaxMax>,
+                                                            threads), threads, 0, s>>>(a);
+        break;
+    }
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+template <typename T>
+int accumulate_impl(T *out, long long n_frames, long long H, long long W, const T *lines,
+                    long long n_lines, const void *terms, int term_bytes, const void *frames,
+                    int frame_bytes, long long n_terms, T max_val, int kernel, int in_overlap,
+                    int out_overlap, void *workspace, size_t ws_bytes, long long ck_capacity,
+                    long long table_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0 || n_terms < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (kernel < CBC_BIWEIGHT || kernel > CBC_TRIANGULAR)
+        return fail(CBC_ERR_INVALID, "kernel is missing");
+    if ((in_overlap != CBC_SUM && in_overlap != CBC_MAX) ||
+        (out_overlap != CBC_SUM && out_overlap != CBC_MAX))
+        return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if ((term_bytes != 4 && term_bytes != 8) || (frame_bytes != 4 && frame_bytes != 8))
+        return fail(CBC_ERR_INVALID, "term_bytes and frame_bytes must be 4 or 8");
+    if (n_lines > 0 && (!terms || !lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_terms > 0 && !frames) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_lines > INT_MAX || n_terms > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines or terms");
+    if (H * W > (long long)UINT_MAX) return fail(CBC_ERR_INVALID, "frames larger than 2^32 pixels");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
+    const int mode = (in_overlap == CBC_MAX ? 1 : 0) | (out_overlap == CBC_MAX ? 2 : 0);
+    const bool table = mode == kAccMaxSum || mode == kAccSumMax;
+    if (table && (table_capacity < 1 || (table_capacity & (table_capacity - 1))))
+        return fail(CBC_ERR_INVALID, "table_capacity must be a power of two");
+    if (!table) table_capacity = 0;
+    const long long pixels = n_frames * H * W;
+    if (n_lines > 0 && pixels > 0 && !out) return fail(CBC_ERR_INVALID, "null pointer");
+    AccLayout L = acc_layout(n_lines, n_terms, ck_capacity, table_capacity, sizeof(LineRec<T>),
+                             sizeof(Checkpoint<T>), sizeof(T));
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    int *frame_of_line = reinterpret_cast<int *>(ws + L.frame_of_line);
+    int *term_of_line = reinterpret_cast<int *>(ws + L.term_of_line);
+    int *frame_of_term = reinterpret_cast<int *>(ws + L.frame_of_term);
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + L.keys);
+    T *vals = reinterpret_cast<T *>(ws + L.vals);
+
+    init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && n_terms > 0) {
+        const unsigned nb = (unsigned)((n_terms + kThreads - 1) / kThreads);
+        if (frame_bytes == 8)
+            frames_check_kernel<int64_t><<<nb, kThreads, 0, s>>>(
+                static_cast<const int64_t *>(frames), n_terms, n_frames, frame_of_term, st);
+        else
+            frames_check_kernel<int32_t><<<nb, kThreads, 0, s>>>(
+                static_cast<const int32_t *>(frames), n_terms, n_frames, frame_of_term, st);
+        note_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines == 0 || pixels == 0) return CBC_OK;
+    const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
+    if (term_bytes == 8)
+        term_frames_kernel<int64_t><<<nb, kThreads, 0, s>>>(
+            static_cast<const int64_t *>(terms), frame_of_term, n_lines, n_terms, term_of_line,
+            frame_of_line, st);
+    else
+        term_frames_kernel<int32_t><<<nb, kThreads, 0, s>>>(
+            static_cast<const int32_t *>(terms), frame_of_term, n_lines, n_terms, term_of_line,
+            frame_of_line, st);
+    note_launches(1);
+    if (table) {
+        e = cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)table_capacity, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(vals, 0, sizeof(T) * (size_t)table_capacity, s);
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    Geometry g;
+    g.H = (int)H;
+    g.W = (int)W;
+    g.tile_w = g.tile_h = kDefaultTileW;
+    g.tiles_x = g.tiles_y = 1;
+    LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
+    Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
+    prep_kernel<T, int32_t, false, true><<<nb, kThreads, 0, s>>>(
+        lines, frame_of_line, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
+    note_launches(1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    AccArgs<T> a;
+    a.d.recs = recs;
+    a.d.cks = cks;
+    a.d.H = (int)H;
+    a.d.W = (int)W;
+    a.d.st = st;
+    a.d.work = &st->work;
+    a.out = out;
+    a.max_val = max_val;
+    a.term_of_line = term_of_line;
+    a.keys = keys;
+    a.vals = vals;
+    a.mask = table ? (unsigned long long)table_capacity - 1ull : 0ull;
+    switch (kernel) {
+    case CBC_BIWEIGHT:    e = launch_accumulate<T, CBC_BIWEIGHT>(a, mode, s); break;
+    case CBC_GAUSSIAN:    e = launch_accumulate<T, CBC_GAUSSIAN>(a, mode, s); break;
+    case CBC_PARABOLIC:   e = launch_accumulate<T, CBC_PARABOLIC>(a, mode, s); break;
+    case CBC_RECTANGULAR: e = launch_accumulate<T, CBC_RECTANGULAR>(a, mode, s); break;
+    default:              e = launch_accumulate<T, CBC_TRIANGULAR>(a, mode, s); break;
+    }
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (table) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long blocks = (table_capacity + kThreads - 1) / kThreads;
+        const long long most = (long long)(sms > 0 ? sms : 132) * 8;
+        if (blocks > most) blocks = most;
+        if (mode == kAccSumMax)
+            merge_kernel<T, 1><<<(unsigned)blocks, kThreads, 0, s>>>(out, keys, vals, table_capacity,
+                                                                     frame_of_term, H * W, st);
+        else
+            merge_kernel<T, 0><<<(unsigned)blocks, kThreads, 0, s>>>(out, keys, vals, table_capacity,
+                                                                     frame_of_term, H * W, st);
+        note_launches(1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return CBC_OK;
+}
+
+}  // namespace cbc
+
+extern "C" {
+
+size_t cbc_accumulate_lines_workspace_size(int64_t n_lines, int64_t n_terms,
+                                           int64_t checkpoint_capacity, int64_t table_capacity,
+                                           int32_t elem_bytes)
+{
+    if (n_lines < 0 || n_terms < 0 || checkpoint_capacity < 0 || table_capacity < 0 ||
+        (elem_bytes != 4 && elem_bytes != 8))
+        return 0;
+    const size_t rec = elem_bytes == 4 ? sizeof(cbc::LineRec<float>) : sizeof(cbc::LineRec<double>);
+    const size_t ck = elem_bytes == 4 ? sizeof(cbc::Checkpoint<float>) : sizeof(cbc::Checkpoint<double>);
+    return cbc::acc_layout(n_lines, n_terms, checkpoint_capacity, table_capacity, rec, ck,
+                           (size_t)elem_bytes).total;
+}
+
+int cbc_accumulate_lines_f32(float *out, int64_t n_frames, int64_t height, int64_t width,
+                             const float *lines, int64_t n_lines, const void *terms,
+                             int32_t term_bytes, const void *frames, int32_t frame_bytes,
+                             int64_t n_terms, float max_val, int32_t kernel, int32_t in_overlap,
+                             int32_t out_overlap, void *workspace, size_t workspace_bytes,
+                             int64_t checkpoint_capacity, int64_t table_capacity, void *stream)
+{
+    return cbc::accumulate_impl<float>(out, n_frames, height, width, lines, n_lines, terms,
+                                       term_bytes, frames, frame_bytes, n_terms, max_val, kernel,
+                                       in_overlap, out_overlap, workspace, workspace_bytes,
+                                       checkpoint_capacity, table_capacity, stream);
+}
+
+int cbc_accumulate_lines_f64(double *out, int64_t n_frames, int64_t height, int64_t width,
+                             const double *lines, int64_t n_lines, const void *terms,
+                             int32_t term_bytes, const void *frames, int32_t frame_bytes,
+                             int64_t n_terms, double max_val, int32_t kernel, int32_t in_overlap,
+                             int32_t out_overlap, void *workspace, size_t workspace_bytes,
+                             int64_t checkpoint_capacity, int64_t table_capacity, void *stream)
+{
+    return cbc::accumulate_impl<double>(out, n_frames, height, width, lines, n_lines, terms,
+                                        term_bytes, frames, frame_bytes, n_terms, max_val, kernel,
+                                        in_overlap, out_overlap, workspace, workspace_bytes,
+                                        checkpoint_capacity, table_capacity, stream);
+}
+
+}  // extern "C"

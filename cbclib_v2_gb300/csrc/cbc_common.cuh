@@ -22,7 +22,8 @@ constexpr int kMaxChunk = 32;
 constexpr int kDefaultTileW = 64;
 constexpr int kDefaultTileH = 64;
 constexpr int kDefaultChunk = 16;
-constexpr int kFatal = (1 << CBC_ERR_INDEX) | (1 << CBC_ERR_CAPACITY) | (1 << CBC_ERR_RANGE);
+constexpr int kFatal = (1 << CBC_ERR_INDEX) | (1 << CBC_ERR_CAPACITY) | (1 << CBC_ERR_RANGE) |
+                       (1 << CBC_ERR_TERM);
 constexpr int kInvalidEntry = INT_MIN;
 
 /* ---- per-line walk record ------------------------------------------------------ */

@@ -17,7 +17,7 @@ import torch
 from . import _native
 from . import device as _device
 
-__all__ = ['draw_lines', 'draw_lines_csr', 'Workspace', 'tuning']
+__all__ = ['draw_lines', 'draw_lines_csr', 'accumulate_lines', 'Workspace', 'tuning']
 
 _tls = threading.local()
 
@@ -274,23 +274,32 @@ def draw_lines(out, lines, idxs=None, max_val: float = 1.0, kernel: str = 'recta
         ``out``.
     """
     k, ov = _check_names(kernel, overlap)
+    return _on_device(out, 'draw_lines',
+                      lambda dev_out: _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov))
+
+
+def _on_device(out, name: str, run):
+    """Run ``run(cuda_tensor)`` on ``out``: CUDA tensors and ``__cuda_array_interface__``
+    arrays in place; host arrays (NumPy, CPU tensors) staged through the GPU and written
+    back, while the current device is 'cuda'.  Returns ``out``."""
     if isinstance(out, torch.Tensor):
         if out.is_cuda:
-            return _draw_lines_cuda(out, lines, idxs, max_val, k, ov)
+            run(out)
+            return out
         host = out
     elif hasattr(out, '__cuda_array_interface__'):
-        _draw_lines_cuda(torch.as_tensor(out, device='cuda'), lines, idxs, max_val, k, ov)
+        run(torch.as_tensor(out, device='cuda'))
         return out
     else:
         host = out
     if _device.get_device() != 'cuda':
-        raise RuntimeError("cbclib_v2_gb300 has no CPU implementation of draw_lines: select "
+        raise RuntimeError(f"cbclib_v2_gb300 has no CPU implementation of {name}: select "
                            "the 'cuda' device or pass CUDA arrays")
     if isinstance(host, torch.Tensor):
         if host.dtype not in (torch.float32, torch.float64):
             raise TypeError(f"out must be float32 or float64, got {host.dtype}")
         dev_out = host.to('cuda')
-        _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov)
+        run(dev_out)
         host.copy_(dev_out)
         return out
     if not isinstance(host, np.ndarray):
@@ -298,9 +307,121 @@ def draw_lines(out, lines, idxs=None, max_val: float = 1.0, kernel: str = 'recta
     if host.dtype not in (np.float32, np.float64):
         raise TypeError(f"out must be float32 or float64, got {host.dtype}")
     dev_out = torch.from_numpy(np.ascontiguousarray(host)).to('cuda')
-    _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov)
+    run(dev_out)
     if host.flags.c_contiguous and host.flags.writeable:
         torch.from_numpy(host).copy_(dev_out)
     else:
         np.copyto(host, dev_out.cpu().numpy())
     return out
+
+
+def _as_device_ints(a, name: str, dev: torch.device) -> torch.Tensor:
+    t = torch.as_tensor(a)
+    if t.is_floating_point() or t.is_complex() or t.dtype == torch.bool:
+        raise TypeError(f"{name} must be an integer array")
+    t = t.reshape(-1)
+    if t.dtype not in (torch.int32, torch.int64):
+        t = t.to(torch.int64)
+    return t.to(device=dev).contiguous()
+
+
+def _table_capacity(ln: torch.Tensor) -> int:
+    """A power of two about twice an upper estimate of the (line, pixel) pairs the
+    lines draw: (long extent + 2w + 3) columns of (3w + 2) pixels each."""
+    d = (ln[:, 2:4] - ln[:, 0:2]).abs()
+    w = ln[:, 4].clamp(min=0)
+    est = float(((d.max(dim=1).values + 2 * w + 3) * (3 * w + 2)).sum().item())
+    need = max(1024, int(2 * est))
+    return 1 << (need - 1).bit_length()
+
+
+def _accumulate_lines_cuda(out: torch.Tensor, lines, terms, frames, max_val: float, kernel: int,
+                           in_ov: int, out_ov: int) -> torch.Tensor:
+    F, H, W = _frames_of(out)
+    dev = out.device
+    ln = _as_device_lines(lines, dev, out.dtype)
+    n_lines = ln.shape[0]
+    tm = _as_device_ints(terms, 'terms', dev)
+    if tm.numel() != n_lines:
+        raise ValueError(f"Term indices ({tm.numel()}) is incompatible with number of lines "
+                         f"({n_lines})")
+    fr = _as_device_ints(frames, 'frames', dev)
+    n_terms = fr.numel()
+    work = out if out.is_contiguous() else out.contiguous()
+    elem = 4 if out.dtype == torch.float32 else 8
+    lib = _native.lib()
+    fn = lib.cbc_accumulate_lines_f32 if elem == 4 else lib.cbc_accumulate_lines_f64
+    table = in_ov != out_ov
+    with torch.cuda.device(dev):
+        stream = torch.cuda.current_stream(dev)
+        key = ('accumulate', dev.index, stream.cuda_stream, threading.get_ident())
+        with _ws_lock:
+            ws = _workspaces.setdefault(key, Workspace(dev))
+        ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
+        table_cap = max(ws.capacity, _table_capacity(ln)) if (table and n_lines) else 0
+        for _ in range(6):
+            nbytes = lib.cbc_accumulate_lines_workspace_size(n_lines, n_terms, ck_capacity,
+                                                             table_cap, elem)
+            buf = ws.ensure(nbytes)
+            rc = fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines, tm.data_ptr(),
+                    tm.element_size(), fr.data_ptr(), fr.element_size(), n_terms, max_val,
+                    kernel, in_ov, out_ov, buf.data_ptr(), buf.numel(), ck_capacity, table_cap,
+                    stream.cuda_stream)
+            if rc:
+                _raise_rc(rc)
+            st = _native.Status()
+            if lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream):
+                _raise_rc(_native.CBC_ERR_CUDA)
+            ws.last_status = st
+            if st.has(_native.CBC_ERR_INDEX):
+                raise IndexError(f"frames range ({int(fr.min())}, {int(fr.max())}) is outside of "
+                                 f"(0, {F})")
+            if st.has(_native.CBC_ERR_TERM):
+                raise IndexError(f"Term index {int(tm[st.bad_line])} is out of range "
+                                 f"(0, {n_terms})")
+            _raise_status(st, F)
+            if not st.has(_native.CBC_ERR_CAPACITY):
+                ws.ck_capacity = ck_capacity
+                ws.capacity = table_cap
+                break
+            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
+            if table:
+                table_cap = max(table_cap, int(st.pairs_needed))
+            if ck_capacity > 2**31 - 1:
+                raise MemoryError("too many walk checkpoints for one call")
+        else:
+            raise RuntimeError("workspace capacity did not converge")
+    if work is not out:
+        out.copy_(work)
+    return out
+
+
+def accumulate_lines(out, lines, terms, frames, max_val: float = 1.0,
+                     kernel: str = 'rectangular', in_overlap: str = 'sum',
+                     out_overlap: str = 'sum'):
+    """Accumulate thick lines grouped into terms across frames (reference:
+    cbclib_v2/_src/functions.py:195-233).
+
+    Args:
+        out: Output frames (..., H, W), float32 or float64, updated in place (CUDA
+            arrays on their device; host arrays staged while the device is 'cuda').
+        lines: (N, 5) rows [x0, y0, x1, y1, width], xy order.
+        terms: (N,) term index of each line.
+        frames: (T,) frame index of each term into the flattened leading dims of ``out``.
+        max_val: peak value of a line's profile.
+        kernel: 'biweight', 'gaussian', 'parabolic', 'rectangular' or 'triangular'.
+        in_overlap: how a term combines its own lines, 'sum' or 'max'.
+        out_overlap: how terms combine into ``out``, 'sum' or 'max'.
+
+    Returns:
+        ``out``.
+    """
+    if kernel not in _native.KERNELS:
+        raise ValueError(f"kernel is missing for {kernel}")
+    if in_overlap not in _native.OVERLAPS or out_overlap not in _native.OVERLAPS:
+        raise ValueError(f"Invalid overlap keyword: {in_overlap}, {out_overlap}")
+    k = _native.KERNELS[kernel]
+    iov, oov = _native.OVERLAPS[in_overlap], _native.OVERLAPS[out_overlap]
+    return _on_device(out, 'accumulate_lines',
+                      lambda dev_out: _accumulate_lines_cuda(dev_out, lines, terms, frames,
+                                                             max_val, k, iov, oov))

@@ -37,6 +37,8 @@ extern "C" {
 #define CBC_ERR_CAPACITY    3   /* pair buffer too small; nothing was drawn, retry      */
 #define CBC_ERR_CUDA        4   /* CUDA runtime error: RuntimeError (cupy_array.hpp:18-24) */
 #define CBC_ERR_RANGE       5   /* a line's walk is longer than CBC_MAX_WALK pixels     */
+#define CBC_ERR_TERM        6   /* accumulate_lines: a term index out of range: IndexError
+                                   (bresenham.cpp:182-188); status flag only          */
 
 #define CBC_MAX_WALK (1 << 22)
 
@@ -194,6 +196,45 @@ CBC_API int cbc_draw_lines_backward_f64(const double *grad_out, int64_t n_frames
                                         int32_t *winner, double *grad_lines, void *workspace,
                                         size_t workspace_bytes, int64_t checkpoint_capacity,
                                         void *stream);
+
+/* accumulate_lines for 2-D lines.  Replaces bresenham.accumulate_lines
+ * (_src/src/bresenham.cpp:301-327, accumulate_lines_nd_impl :151-259) and
+ * cuda_draw_lines.accumulate_lines (_src/src/cuda_draw_lines.cu:1049-1057, 1077-1095).
+ *
+ * Line i belongs to term terms[i] (int32 or int64, term_bytes), term t to frame
+ * frames[t] (frame_bytes); n_terms = length of frames.  Each term's lines are combined
+ * with in_overlap (CBC_SUM / CBC_MAX) in a zeroed buffer, and every pixel the term
+ * drew is merged into out[frames[t]] with out_overlap.  Errors seen on the device set
+ * status flags and leave out untouched: frames outside [0, n_frames) set
+ * CBC_ERR_INDEX (idx_min / idx_max hold the frames' range), a term outside
+ * [0, n_terms) sets CBC_ERR_TERM (bad_line: the first such line).
+ *
+ * The mixed pairs (sum in / max out, max in / sum out) keep per (term, pixel) values
+ * in a hash table of `table_capacity` entries (a power of two; 12 or 16 bytes each)
+ * in the workspace, about twice the number of (term, pixel) pairs drawn.  A full
+ * table sets CBC_ERR_CAPACITY with pairs_needed = a capacity to retry with; so does a
+ * checkpoint overflow, with checkpoints_needed.  The equal pairs use no table. */
+CBC_API size_t cbc_accumulate_lines_workspace_size(int64_t n_lines, int64_t n_terms,
+                                                   int64_t checkpoint_capacity,
+                                                   int64_t table_capacity, int32_t elem_bytes);
+
+CBC_API int cbc_accumulate_lines_f32(float *out, int64_t n_frames, int64_t height,
+                                     int64_t width, const float *lines, int64_t n_lines,
+                                     const void *terms, int32_t term_bytes, const void *frames,
+                                     int32_t frame_bytes, int64_t n_terms, float max_val,
+                                     int32_t kernel, int32_t in_overlap, int32_t out_overlap,
+                                     void *workspace, size_t workspace_bytes,
+                                     int64_t checkpoint_capacity, int64_t table_capacity,
+                                     void *stream);
+
+CBC_API int cbc_accumulate_lines_f64(double *out, int64_t n_frames, int64_t height,
+                                     int64_t width, const double *lines, int64_t n_lines,
+                                     const void *terms, int32_t term_bytes, const void *frames,
+                                     int32_t frame_bytes, int64_t n_terms, double max_val,
+                                     int32_t kernel, int32_t in_overlap, int32_t out_overlap,
+                                     void *workspace, size_t workspace_bytes,
+                                     int64_t checkpoint_capacity, int64_t table_capacity,
+                                     void *stream);
 
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
