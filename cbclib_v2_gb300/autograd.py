@@ -45,6 +45,8 @@ def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[t
     if dtype not in (torch.float32, torch.float64):
         raise TypeError(f"grad_out must be float32 or float64, got {dtype}")
     ln = ndimage._as_device_lines(lines, dev, dtype)
+    if ln.shape[1] != 5:
+        raise ValueError("gradients are implemented for 2-D lines (N, 5)")
     n = ln.shape[0]
     ix = ndimage._as_device_idxs(idxs, n, dev)
     H, W = int(grad_out.shape[-2]), int(grad_out.shape[-1])

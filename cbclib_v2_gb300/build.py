@@ -11,8 +11,8 @@ CSRC = os.path.join(PKG, 'csrc')
 INCLUDE = os.path.join(ROOT, 'include')
 LIBDIR = os.path.join(PKG, '_lib')
 LIB = os.path.join(LIBDIR, 'libcbc_gb300.so')
-SOURCES = ['cbc_draw_lines.cu', 'cbc_adjoint.cu', 'cbc_accumulate.cu']
-DEPS = ['exact.cuh', 'exp_table.inc', 'cbc_common.cuh']
+SOURCES = ['cbc_draw_lines.cu', 'cbc_adjoint.cu', 'cbc_accumulate.cu', 'cbc_lines3d.cu']
+DEPS = ['exact.cuh', 'exp_table.inc', 'cbc_common.cuh', 'cbc_accumulate.cuh']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

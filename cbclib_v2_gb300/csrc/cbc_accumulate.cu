@@ -25,45 +25,9 @@
 #include <limits.h>
 #include <string>
 
-#include "cbc_common.cuh"
+#include "cbc_accumulate.cuh"
 
 namespace cbc {
-
-/* bit 0: terms combine their lines by max; bit 1: terms merge into out by max
- * (the Update encoding of bresenham.cpp:304-307) */
-enum : int { kAccSumSum = 0, kAccMaxSum = 1, kAccSumMax = 2, kAccMaxMax = 3 };
-
-constexpr unsigned long long kEmptyKey = ~0ull;
-constexpr int kMaxProbe = 64;
-
-/* splitmix64's finaliser (Steele, Lea and Flood 2014) as the table's hash */
-__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
-{
-    x ^= x >> 30;
-    x *= 0xbf58476d1ce4e5b9ull;
-    x ^= x >> 27;
-    x *= 0x94d049bb133111ebull;
-    x ^= x >> 31;
-    return x;
-}
-
-/* std::max(buffer, v) with buffer starting at +0, as an atomic on the slot's value */
-template <typename T>
-__device__ __forceinline__ void term_combine_max(T *slot, T v);
-
-template <>
-__device__ __forceinline__ void term_combine_max<float>(float *slot, float v)
-{
-    /* the slot holds +0 or a positive value: only v > 0 can change it, and positive
-     * floats order as their bit patterns (NaN and negative v leave it unchanged) */
-    if (v > 0.0f) atomicMax(reinterpret_cast<int *>(slot), __float_as_int(v));
-}
-
-template <>
-__device__ __forceinline__ void term_combine_max<double>(double *slot, double v)
-{
-    if (v > 0.0) atomicMax(reinterpret_cast<long long *>(slot), __double_as_longlong(v));
-}
 
 template <typename T, int K, int MODE>
 struct AccumAct {
@@ -89,22 +53,7 @@ struct AccumAct {
         } else if (MODE == kAccMaxMax) {
             global_combine_max(out + S.fbase[slot] + pix, T(0) < v ? v : T(0));
         } else {
-            const unsigned long long key =
-                ((unsigned long long)(unsigned)term_of_line[S.line[slot]] << 32) |
-                (unsigned long long)(unsigned)pix;
-            unsigned long long h = mix64(key) & mask;
-            for (int probe = 0; probe < kMaxProbe; probe++) {
-                unsigned long long k = *reinterpret_cast<volatile unsigned long long *>(keys + h);
-                if (k == kEmptyKey) k = atomicCAS(keys + h, kEmptyKey, key);
-                if (k == kEmptyKey || k == key) {
-                    if (MODE & 1) term_combine_max(vals + h, v);
-                    else atomicAdd(vals + h, v);
-                    return;
-                }
-                h = (h + 1) & mask;
-            }
-            atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
-            atomicMax(&st->pairs, 4ull * (mask + 1));
+            table_combine<T, MODE & 1>(keys, vals, mask, term_of_line[S.line[slot]], pix, v, st);
         }
     }
 };
@@ -135,86 +84,6 @@ accumulate_kernel(AccArgs<T> a)
     act.mask = a.mask;
     act.st = a.d.st;
     drive_segments(a.d, act);
-}
-
-/* every frames[t] in [0, n_frames) (bresenham.cpp:23-36: "frames range (min, max) is
- * outside of (0, n_frames)"); the int32 copy feeds the merge */
-template <typename FI>
-__global__ void __launch_bounds__(kThreads)
-frames_check_kernel(const FI *__restrict__ frames, long long n_terms, long long n_frames,
-                    int *__restrict__ frame_of_term, DevStatus *st)
-{
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = t < n_terms;
-    const long long f = in ? (long long)frames[t] : 0;
-    warp_minmax(f, in, st);
-    if (!in) return;
-    if (f < 0 || f >= n_frames) atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
-    frame_of_term[t] = (f >= 0 && f < n_frames) ? (int)f : 0;
-}
-
-/* per line: its term (bresenham.cpp:182-188: "Term index t is out of range (0, T)")
- * and its frame */
-template <typename TI>
-__global__ void __launch_bounds__(kThreads)
-term_frames_kernel(const TI *__restrict__ terms, const int *__restrict__ frame_of_term,
-                   long long n_lines, long long n_terms, int *__restrict__ term_of_line,
-                   int *__restrict__ frame_of_line, DevStatus *st)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_lines) return;
-    const long long t = (long long)terms[i];
-    if (t < 0 || t >= n_terms) {
-        atomicOr(&st->flags, 1 << CBC_ERR_TERM);
-        atomicMin(&st->bad_line, (unsigned long long)i);
-        term_of_line[i] = 0;
-        frame_of_line[i] = 0;
-        return;
-    }
-    term_of_line[i] = (int)t;
-    frame_of_line[i] = frame_of_term[t];
-}
-
-/* the table's entries merged into out with out_overlap (sum: out = v + out;
- * max: out = std::max(out, v)); nothing when the call has failed */
-template <typename T, int OUT_MAX>
-__global__ void __launch_bounds__(kThreads)
-merge_kernel(T *__restrict__ out, const unsigned long long *__restrict__ keys,
-             const T *__restrict__ vals, long long cap, const int *__restrict__ frame_of_term,
-             long long frame_px, const DevStatus *st)
-{
-    if (st->flags & kFatal) return;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
-         i += (long long)gridDim.x * blockDim.x) {
-        const unsigned long long k = keys[i];
-        if (k == kEmptyKey) continue;
-        const int term = (int)(k >> 32);
-        T *dst = out + (long long)frame_of_term[term] * frame_px + (long long)(k & 0xffffffffull);
-        if (OUT_MAX) global_combine_max(dst, vals[i]);
-        else atomicAdd(dst, vals[i]);
-    }
-}
-
-struct AccLayout {
-    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals, total;
-};
-
-AccLayout acc_layout(long long n_lines, long long n_terms, long long ck_capacity,
-                     long long table_capacity, size_t rec_bytes, size_t ck_bytes, size_t elem)
-{
-    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
-    AccLayout L;
-    size_t off = 0;
-    L.status = off;        off = up(off + sizeof(DevStatus));
-    L.recs = off;          off = up(off + rec_bytes * (size_t)n_lines);
-    L.cks = off;           off = up(off + ck_bytes * (size_t)ck_capacity);
-    L.frame_of_line = off; off = up(off + sizeof(int) * (size_t)n_lines);
-    L.term_of_line = off;  off = up(off + sizeof(int) * (size_t)n_lines);
-    L.frame_of_term = off; off = up(off + sizeof(int) * (size_t)n_terms);
-    L.keys = off;          off = up(off + sizeof(unsigned long long) * (size_t)table_capacity);
-    L.vals = off;          off = up(off + elem * (size_t)table_capacity);
-    L.total = off;
-    return L;
 }
 
 template <typename T, int K>
@@ -290,34 +159,15 @@ int accumulate_impl(T *out, long long n_frames, long long H, long long W, const 
     init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);
     note_launches(1);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && n_terms > 0) {
-        const unsigned nb = (unsigned)((n_terms + kThreads - 1) / kThreads);
-        if (frame_bytes == 8)
-            frames_check_kernel<int64_t><<<nb, kThreads, 0, s>>>(
-                static_cast<const int64_t *>(frames), n_terms, n_frames, frame_of_term, st);
-        else
-            frames_check_kernel<int32_t><<<nb, kThreads, 0, s>>>(
-                static_cast<const int32_t *>(frames), n_terms, n_frames, frame_of_term, st);
-        note_launches(1);
-        e = cudaGetLastError();
-    }
+    if (e == cudaSuccess)
+        e = launch_frames_check(frames, frame_bytes, n_terms, n_frames, frame_of_term, st, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines == 0 || pixels == 0) return CBC_OK;
     const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
-    if (term_bytes == 8)
-        term_frames_kernel<int64_t><<<nb, kThreads, 0, s>>>(
-            static_cast<const int64_t *>(terms), frame_of_term, n_lines, n_terms, term_of_line,
-            frame_of_line, st);
-    else
-        term_frames_kernel<int32_t><<<nb, kThreads, 0, s>>>(
-            static_cast<const int32_t *>(terms), frame_of_term, n_lines, n_terms, term_of_line,
-            frame_of_line, st);
-    note_launches(1);
-    if (table) {
-        e = cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)table_capacity, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(vals, 0, sizeof(T) * (size_t)table_capacity, s);
-        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    }
+    e = launch_term_frames(terms, term_bytes, frame_of_term, n_lines, n_terms, term_of_line,
+                           frame_of_line, st, s);
+    if (e == cudaSuccess && table) e = clear_table(keys, vals, table_capacity, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     Geometry g;
     g.H = (int)H;
     g.W = (int)W;
@@ -352,20 +202,8 @@ int accumulate_impl(T *out, long long n_frames, long long H, long long W, const 
     }
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (table) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        long long blocks = (table_capacity + kThreads - 1) / kThreads;
-        const long long most = (long long)(sms > 0 ? sms : 132) * 8;
-        if (blocks > most) blocks = most;
-        if (mode == kAccSumMax)
-            merge_kernel<T, 1><<<(unsigned)blocks, kThreads, 0, s>>>(out, keys, vals, table_capacity,
-                                                                     frame_of_term, H * W, st);
-        else
-            merge_kernel<T, 0><<<(unsigned)blocks, kThreads, 0, s>>>(out, keys, vals, table_capacity,
-                                                                     frame_of_term, H * W, st);
-        note_launches(1);
-        e = cudaGetLastError();
+        e = launch_merge(out, keys, vals, table_capacity, frame_of_term, H * W,
+                         mode == kAccSumMax, st, s);
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     }
     return CBC_OK;

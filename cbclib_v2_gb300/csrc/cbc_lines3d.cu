@@ -1,0 +1,727 @@
+/*
+ * cbc_lines3d.cu — draw_lines and accumulate_lines for 3-D lines (L = 7:
+ * [x0, y0, z0, x1, y1, z1, width]) into volumes (F, D, H, W).
+ *
+ * Reference: the N = 3 instantiation of draw_lines_nd_impl / accumulate_lines_nd_impl
+ * (cbclib_v2/_src/src/bresenham.cpp:38-101, :151-259) and its walk draw_line_3d
+ * (bresenham.hpp:389-430) with LineIterator (:117-231) and BresenhamPlotter (:233-296).
+ *
+ * The 3-D walk visits, at every step of the long axis, the centre voxel and then four
+ * quadrants: a 2-D walk over the two short axes that stays while the normal error is
+ * below width^2, and from each of its voxels a 1-D span along each short axis.  Some
+ * voxels are visited more than once, and with sum overlap each visit adds, as in the
+ * reference.  Here the walk is replayed in the reference's arithmetic: float increments
+ * as round-to-nearest intrinsics, and the error terms the reference rounds through
+ * double (std::pow(T, int) promotes) evaluated in double on the device.
+ *
+ * Work split: prep3_kernel builds each line's record and walks its long axis once,
+ * storing the exact iterator state at every 8th long-axis column inside the volume;
+ * render3_kernel then gives every (line, 8-column segment) to one thread, which replays
+ * its columns from the checkpoint and combines each drawn voxel into `out` (sum: L2
+ * add; max: std::max merge), or, for accumulate_lines, into the (term, voxel) table or
+ * directly as in the 2-D path.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <limits.h>
+#include <string>
+
+#include "cbc_accumulate.cuh"
+
+namespace cbc {
+namespace l3 {
+
+/* pairs of axes: (0, 1), (0, 2), (1, 2) (UniquePairs<3>, geometry.hpp:403-448) */
+__device__ __constant__ const int kPairA[3] = {0, 0, 1};
+__device__ __constant__ const int kPairB[3] = {1, 2, 2};
+
+template <typename T>
+struct Rec3 {
+    T tau[3];            /* pt1 - pt0                                   */
+    T nrm[3][3];         /* normal of pair k, non-zero on its two axes  */
+    T len, len2, w, ww;
+    int32_t mpt1[3];     /* walk end (the reference adds one step)      */
+    int32_t step[3];
+    int32_t axis, frame, flags;
+    int32_t c0, ncols, ck_base;
+};
+
+/* LineIterator state; `next` is recomputed from it by update() */
+template <typename T>
+struct It3 {
+    int32_t cur[3];
+    int32_t step[3];
+    bool next[3];
+    T te;
+    T ne[3];
+};
+
+template <typename T>
+struct Ck3 {
+    int32_t cur[3];
+    int32_t line;
+    T te;
+    T ne[3];
+    int32_t seg;
+    int32_t pad;
+};
+
+/* LineIterator::update with NormalError::is_next (bresenham.hpp:98-111, :205-220) */
+template <typename T>
+__device__ __forceinline__ void update(const Rec3<T> &r, It3<T> &it)
+{
+    using A = Ar<T>;
+    #pragma unroll
+    for (int i = 0; i < 3; i++) it.next[i] = it.step[i] != 0;
+    #pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int a1 = kPairA[k], a2 = kPairB[k];
+        if (it.step[a1] && it.step[a2]) {
+            const T d1 = it.step[a1] > 0 ? r.nrm[k][a1] : -r.nrm[k][a1];
+            const T d2 = it.step[a2] > 0 ? r.nrm[k][a2] : -r.nrm[k][a2];
+            const T ex = A::add(it.ne[k], d1);
+            const T ey = A::add(it.ne[k], d2);
+            const T exy = A::add(ex, d2);
+            bool f, s;
+            if (fabs(ey) < fabs(ex)) { f = fabs(exy) < fabs(ey); s = true; }
+            else                     { f = true; s = fabs(exy) < fabs(ex); }
+            it.next[a1] = it.next[a1] && f;
+            it.next[a2] = it.next[a2] && s;
+        }
+    }
+}
+
+/* LineIterator::increment by one step along `axis` (bresenham.hpp:195-203) */
+template <typename T>
+__device__ __forceinline__ void increment(const Rec3<T> &r, It3<T> &it, int axis)
+{
+    using A = Ar<T>;
+    const int x = it.step[axis];
+    it.cur[axis] += x;
+    it.te = A::add(it.te, x > 0 ? r.tau[axis] : -r.tau[axis]);
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (kPairA[k] == axis || kPairB[k] == axis)
+            it.ne[k] = A::add(it.ne[k], x > 0 ? r.nrm[k][axis] : -r.nrm[k][axis]);
+}
+
+template <typename T>
+__device__ __forceinline__ void advance(const Rec3<T> &r, It3<T> &it)    /* operator++ */
+{
+    #pragma unroll
+    for (int i = 0; i < 3; i++)
+        if (it.next[i]) increment(r, it, i);
+    update(r, it);
+}
+
+template <typename T>
+__device__ __forceinline__ bool at_end(const Rec3<T> &r, const It3<T> &it)
+{
+    return it.cur[0] == r.mpt1[0] || it.cur[1] == r.mpt1[1] || it.cur[2] == r.mpt1[2];
+}
+
+/* BresenhamPlotter::normal_error (bresenham.hpp:284-289): a T accumulator fed with the
+ * double squares of ne / len */
+template <typename T>
+__device__ __forceinline__ T normal_error(const Rec3<T> &r, const It3<T> &it)
+{
+    using A = Ar<T>;
+    T err = T(0);
+    #pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double b = (double)A::div(it.ne[k], r.len);
+        err = (T)__dadd_rn((double)err, __dmul_rn(b, b));
+    }
+    return err;
+}
+
+/* BresenhamPlotter::error (bresenham.hpp:291-296) */
+template <typename T>
+__device__ __forceinline__ T error(const Rec3<T> &r, const It3<T> &it)
+{
+    using A = Ar<T>;
+    const T m1 = -it.te, m2 = A::sub(it.te, r.len2);
+    T ta = m1 < m2 ? m2 : m1;
+    ta = ta < T(0) ? T(0) : ta;
+    const double a = (double)A::div(ta, r.len);
+    const double e = __dadd_rn(__dmul_rn(a, a), (double)normal_error(r, it));
+    return (T)__ddiv_rn(e, (double)r.ww);
+}
+
+/* BresenhamPlotter construction and begin() (bresenham.hpp:243-263) */
+template <typename T>
+__device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
+{
+    using A = Ar<T>;
+    too_long = false;
+    T p0[3], p1[3];
+    for (int i = 0; i < 3; i++) { p0[i] = ln[i]; p1[i] = ln[3 + i]; }
+    const T w = ln[6];
+    for (int i = 0; i < 7; i++)
+        if (!isfinite(ln[i])) return false;
+    if (!(w > T(0))) return false;                 /* error() is +inf everywhere */
+    for (int i = 0; i < 3; i++) r.tau[i] = A::sub(p1[i], p0[i]);
+    int ax = 0;
+    for (int i = 1; i < 3; i++)
+        if (fabs(r.tau[ax]) < fabs(r.tau[i])) ax = i;
+    r.axis = ax;
+    T mag = T(0);
+    for (int i = 0; i < 3; i++) mag = A::add(mag, A::mul(r.tau[i], r.tau[i]));
+    r.len = A::sqrt(mag);
+    if (!(r.len > T(0))) return false;
+    const T ceilw = A::add(ceil(w), T(1));
+    if (!(ceilw < T(1e9))) return false;
+    T tn[3];
+    for (int i = 0; i < 3; i++) tn[i] = A::div(r.tau[i], r.len);
+    const T scale = fabs(A::div(ceilw, tn[ax]));
+    int32_t mpt0[3];
+    const T lim = T(1 << 30);
+    for (int i = 0; i < 3; i++) {
+        r.step[i] = (p1[i] >= p0[i]) ? 1 : -1;
+        const T a = round(A::sub(p0[i], A::mul(scale, tn[i])));
+        const T b = round(A::add(p1[i], A::mul(scale, tn[i])));
+        if (!(fabs(a) < lim && fabs(b) < lim)) { too_long = true; return false; }
+        mpt0[i] = (int32_t)a;
+        r.mpt1[i] = (int32_t)b + r.step[i];
+    }
+    long long walk = (long long)r.mpt1[ax] - mpt0[ax];
+    if (walk < 0) walk = -walk;
+    const T span = A::div(A::mul(w, r.len), fabs(r.tau[ax]));
+    if (walk > CBC_MAX_WALK || !(span < T(CBC_MAX_WALK))) { too_long = true; return false; }
+    for (int k = 0; k < 3; k++)
+        for (int i = 0; i < 3; i++) r.nrm[k][i] = T(0);
+    for (int k = 0; k < 3; k++) {
+        const int a1 = kPairA[k], a2 = kPairB[k];
+        r.nrm[k][a1] = A::sub(p1[a2], p0[a2]);
+        r.nrm[k][a2] = A::sub(p0[a1], p1[a1]);
+    }
+    r.len2 = A::mul(r.len, r.len);
+    r.w = w;
+    r.ww = A::mul(w, w);
+    T d[3];
+    for (int i = 0; i < 3; i++) d[i] = A::sub((T)mpt0[i], p0[i]);
+    it.te = T(0);
+    for (int i = 0; i < 3; i++) it.te = A::add(it.te, A::mul(r.tau[i], d[i]));
+    for (int k = 0; k < 3; k++) {
+        T e = T(0);
+        for (int i = 0; i < 3; i++) e = A::add(e, A::mul(r.nrm[k][i], d[i]));
+        it.ne[k] = e;
+    }
+    for (int i = 0; i < 3; i++) { it.cur[i] = mpt0[i]; it.step[i] = r.step[i]; }
+    update(r, it);
+    r.flags = kDrawable;
+    return true;
+}
+
+struct Vol {
+    int D, H, W;
+    __device__ int ext(int axis) const { return axis == 0 ? W : (axis == 1 ? H : D); }
+};
+
+template <typename IdxT>
+__device__ __forceinline__ long long load_frame(const void *idxs, long long i, long long n_frames)
+{
+    if (!idxs) return n_frames == 1 ? 0 : i;
+    return (long long)static_cast<const IdxT *>(idxs)[i];
+}
+
+/* line records, frame checks and the long-axis checkpoints of every line */
+template <typename T, typename IdxT>
+__global__ void __launch_bounds__(kThreads)
+prep3_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
+             long long n_frames, Vol v, Rec3<T> *__restrict__ recs, Ck3<T> *__restrict__ cks,
+             long long ck_capacity, DevStatus *st)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < n_lines;
+    long long frame = in ? load_frame<IdxT>(idxs, i, n_frames) : 0;
+    if (idxs) warp_minmax(frame, in, st);
+    Rec3<T> r;
+    It3<T> it;
+    r.flags = 0;
+    r.ncols = 0;
+    int nck = 0, lmin = 0, lmax = -1, sa = 1;
+    if (in) {
+        if (frame < 0 || frame >= n_frames) {
+            atomicOr(&st->flags, 1 << CBC_ERR_INDEX);
+            atomicMin(&st->bad_line, (unsigned long long)i);
+        } else {
+            bool too_long = false;
+            if (build_rec3(lines + 7 * i, r, it, too_long)) {
+                r.frame = (int32_t)frame;
+                const int ax = r.axis;
+                sa = r.step[ax];
+                const int first = it.cur[ax], last = r.mpt1[ax] - sa;
+                lmin = max(min(first, last), 0);
+                lmax = min(max(first, last), v.ext(ax) - 1);
+                if (lmin <= lmax) {
+                    r.ncols = lmax - lmin + 1;
+                    r.c0 = sa > 0 ? lmin : lmax;
+                    nck = (r.ncols + kSeg - 1) / kSeg;
+                } else {
+                    r.flags = 0;
+                }
+            } else if (too_long) {
+                atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+                atomicMin(&st->bad_line, (unsigned long long)i);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31;
+    int incl = nck;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    unsigned long long wbase = 0;
+    if (lane == 31) wbase = atomicAdd(&st->cks, (unsigned long long)incl);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    if (!in) return;
+    if (nck > 0) {
+        const unsigned long long cb = wbase + (unsigned long long)(incl - nck);
+        if (cb + (unsigned long long)nck > (unsigned long long)ck_capacity) {
+            atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+            nck = 0;
+            r.flags = 0;
+        } else {
+            r.ck_base = (int32_t)cb;
+        }
+    }
+    if (nck > 0) {
+        /* columns are the positions where the next step moves the long axis; one per
+         * long coordinate.  Checkpoint k holds the state at the column of walk index
+         * k * kSeg (walk index = (c - c0) * step of the long axis). */
+        const int ax = r.axis;
+        int k = 0;
+        long long guard = 0;
+        while (k < nck && !at_end(r, it)) {
+            if (it.next[ax]) {
+                const int idx = (it.cur[ax] - r.c0) * sa;
+                if (idx == k * kSeg) {
+                    Ck3<T> c;
+                    for (int a = 0; a < 3; a++) c.cur[a] = it.cur[a];
+                    c.line = (int32_t)i;
+                    c.te = it.te;
+                    for (int a = 0; a < 3; a++) c.ne[a] = it.ne[a];
+                    c.seg = k;
+                    c.pad = 0;
+                    cks[r.ck_base + k] = c;
+                    k++;
+                }
+            }
+            advance(r, it);
+            if (++guard > 4LL * CBC_MAX_WALK + 64) {
+                atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+                break;
+            }
+        }
+        for (; k < nck; k++) {          /* the walk ended first: empty segments */
+            Ck3<T> c;
+            c.cur[0] = INT_MIN;
+            c.cur[1] = c.cur[2] = 0;
+            c.line = (int32_t)i;
+            c.te = T(0);
+            c.ne[0] = c.ne[1] = c.ne[2] = T(0);
+            c.seg = k;
+            c.pad = 0;
+            cks[r.ck_base + k] = c;
+        }
+    }
+    recs[i] = r;
+}
+
+/* where the drawn voxels go */
+template <typename T, int K>
+struct Emit3 {
+    T *out;
+    T max_val;
+    int mode;                      /* 0 sum, 1 max (draw_lines); accumulate: kAcc* + 4 */
+    const int *term_of_line;
+    unsigned long long *keys;
+    T *vals;
+    unsigned long long mask;
+    DevStatus *st;
+    __device__ __forceinline__ void operator()(long long fbase, long long vox, int line, T E) const {
+        using A = Ar<T>;
+        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
+        switch (mode) {
+        case 0:  atomicAdd(out + fbase + vox, v); break;
+        case 1:  global_combine_max(out + fbase + vox, v); break;
+        case 4 + kAccSumSum: atomicAdd(out + fbase + vox, v); break;
+        case 4 + kAccMaxMax: global_combine_max(out + fbase + vox, T(0) < v ? v : T(0)); break;
+        case 4 + kAccMaxSum:
+            table_combine<T, 1>(keys, vals, mask, term_of_line[line], vox, v, st);
+            break;
+        default:
+            table_combine<T, 0>(keys, vals, mask, term_of_line[line], vox, v, st);
+            break;
+        }
+    }
+};
+
+/* a visited voxel: the error, and for error <= 1 inside the volume, the emit */
+template <typename T, int K>
+__device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, const Vol &v,
+                                      long long fbase, int line, const Emit3<T, K> &emit)
+{
+    const T E = error(r, it);
+    if (!(E <= T(1))) return;
+    if (it.cur[0] < 0 || it.cur[0] >= v.W || it.cur[1] < 0 || it.cur[1] >= v.H ||
+        it.cur[2] < 0 || it.cur[2] >= v.D)
+        return;
+    const long long vox = ((long long)it.cur[2] * v.H + it.cur[1]) * v.W + it.cur[0];
+    emit(fbase, vox, line, E);
+}
+
+template <typename T>
+__device__ __forceinline__ It3<T> collapse(const Rec3<T> &r, const It3<T> &src, int axis)
+{
+    It3<T> it = src;
+    it.step[axis] = 0;
+    update(r, it);
+    return it;
+}
+
+/* one column of draw_line_3d (bresenham.hpp:392-428): the centre voxel and the four
+ * quadrants of the short-axis plane */
+template <typename T, int K>
+__device__ void draw_column(const Rec3<T> &r, const It3<T> &it, const Vol &v, long long fbase,
+                            int line, const Emit3<T, K> &emit, DevStatus *st)
+{
+    const int ax = r.axis, ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
+    visit(r, it, v, fbase, line, emit);
+    long long guard = 0;
+    for (int q = 0; q < 4; q++) {
+        It3<T> ixy = it;
+        ixy.step[ax] = 0;
+        if (q & 1) ixy.step[ax1] = -ixy.step[ax1];
+        if (q >> 1) ixy.step[ax2] = -ixy.step[ax2];
+        update(r, ixy);
+        increment(r, ixy, ((q & 1) ^ (q >> 1)) == 0 ? ax1 : ax2);      /* move */
+        update(r, ixy);
+        for (; normal_error(r, ixy) < r.ww; advance(r, ixy)) {
+            visit(r, ixy, v, fbase, line, emit);
+            for (int j = 1; j < 3; j++) {
+                const int aj = (ax + j) % 3;
+                if (!ixy.next[aj]) continue;
+                It3<T> ix = collapse(r, ixy, aj);
+                for (advance(r, ix); normal_error(r, ix) < r.ww; advance(r, ix)) {
+                    visit(r, ix, v, fbase, line, emit);
+                    if (++guard > 4LL * CBC_MAX_WALK) break;
+                }
+            }
+            if (++guard > 4LL * CBC_MAX_WALK) {
+                atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+                return;
+            }
+        }
+    }
+}
+
+template <typename T>
+struct Render3Args {
+    const Rec3<T> *recs;
+    const Ck3<T> *cks;
+    Vol v;
+    DevStatus *st;
+};
+
+/* one thread per (line, 8-column segment), grid-stride */
+template <typename T, int K>
+__global__ void __launch_bounds__(kThreads)
+render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
+{
+    if (a.st->flags & kFatal) return;
+    const long long total = (long long)a.st->cks;
+    for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += (long long)gridDim.x * blockDim.x) {
+        const Ck3<T> ck = a.cks[item];
+        if (ck.cur[0] == INT_MIN) continue;
+        const Rec3<T> r = a.recs[ck.line];
+        It3<T> it;
+        for (int i = 0; i < 3; i++) { it.cur[i] = ck.cur[i]; it.step[i] = r.step[i]; }
+        it.te = ck.te;
+        for (int i = 0; i < 3; i++) it.ne[i] = ck.ne[i];
+        update(r, it);
+        const int ax = r.axis, sa = r.step[ax];
+        const int lo = ck.seg * kSeg, hi = min(lo + kSeg - 1, r.ncols - 1);
+        const long long fbase = (long long)r.frame * a.v.D * a.v.H * a.v.W;
+        long long guard = 0;
+        while (!at_end(r, it)) {
+            if (it.next[ax]) {
+                const int idx = (it.cur[ax] - r.c0) * sa;
+                if (idx > hi) break;
+                if (idx >= lo) draw_column(r, it, a.v, fbase, ck.line, emit, a.st);
+            }
+            advance(r, it);
+            if (++guard > 4LL * CBC_MAX_WALK + 64) {
+                atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                break;
+            }
+        }
+    }
+}
+
+struct Layout3 {
+    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals, total;
+};
+
+inline Layout3 layout3(long long n_lines, long long n_terms, long long ck_capacity,
+                       long long table_capacity, size_t elem)
+{
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t rec = elem == 4 ? sizeof(Rec3<float>) : sizeof(Rec3<double>);
+    const size_t ck = elem == 4 ? sizeof(Ck3<float>) : sizeof(Ck3<double>);
+    Layout3 L;
+    size_t off = 0;
+    L.status = off;        off = up(off + sizeof(DevStatus));
+    L.recs = off;          off = up(off + rec * (size_t)n_lines);
+    L.cks = off;           off = up(off + ck * (size_t)ck_capacity);
+    L.frame_of_line = off; off = up(off + sizeof(int) * (size_t)n_lines);
+    L.term_of_line = off;  off = up(off + sizeof(int) * (size_t)n_lines);
+    L.frame_of_term = off; off = up(off + sizeof(int) * (size_t)n_terms);
+    L.keys = off;          off = up(off + sizeof(unsigned long long) * (size_t)table_capacity);
+    L.vals = off;          off = up(off + elem * (size_t)table_capacity);
+    L.total = off;
+    return L;
+}
+
+template <typename T, int K>
+cudaError_t launch_render3(const Render3Args<T> &a, const Emit3<T, K> &emit, cudaStream_t s)
+{
+    const unsigned grid = resident_grid(render3_kernel<T, K>, kThreads);
+    render3_kernel<T, K><<<grid, kThreads, 0, s>>>(a, emit);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_render3_k(const Render3Args<T> &a, int kernel, T *out, T max_val, int mode,
+                             const int *term_of_line, unsigned long long *keys, T *vals,
+                             unsigned long long mask, cudaStream_t s)
+{
+#define CBC_L3_CASE(KK)                                                                  \
+    case KK: {                                                                           \
+        Emit3<T, KK> e{out, max_val, mode, term_of_line, keys, vals, mask, a.st};        \
+        return launch_render3<T, KK>(a, e, s);                                           \
+    }
+    switch (kernel) {
+    CBC_L3_CASE(CBC_BIWEIGHT)
+    CBC_L3_CASE(CBC_GAUSSIAN)
+    CBC_L3_CASE(CBC_PARABOLIC)
+    CBC_L3_CASE(CBC_RECTANGULAR)
+    default: {
+        Emit3<T, CBC_TRIANGULAR> e{out, max_val, mode, term_of_line, keys, vals, mask, a.st};
+        return launch_render3<T, CBC_TRIANGULAR>(a, e, s);
+    }
+    }
+#undef CBC_L3_CASE
+}
+
+/* shared by draw and accumulate: frames given per line (int32 frame_of_line or the
+ * caller's idxs), accumulate state when mode >= 4 */
+template <typename T>
+int run3(T *out, long long n_frames, long long D, long long H, long long W, const T *lines,
+         long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel, int mode,
+         unsigned char *ws, const Layout3 &L, long long ck_capacity, long long table_capacity,
+         const int *term_of_line, const int *frame_of_term, cudaStream_t s)
+{
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    Rec3<T> *recs = reinterpret_cast<Rec3<T> *>(ws + L.recs);
+    Ck3<T> *cks = reinterpret_cast<Ck3<T> *>(ws + L.cks);
+    Vol v{(int)D, (int)H, (int)W};
+    const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
+    if (idxs && idx_bytes == 8)
+        prep3_kernel<T, int64_t><<<nb, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, v, recs,
+                                                         cks, ck_capacity, st);
+    else
+        prep3_kernel<T, int32_t><<<nb, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, v, recs,
+                                                         cks, ck_capacity, st);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    Render3Args<T> a{recs, cks, v, st};
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + L.keys);
+    T *vals = reinterpret_cast<T *>(ws + L.vals);
+    const unsigned long long mask = table_capacity > 0 ? (unsigned long long)table_capacity - 1 : 0;
+    e = launch_render3_k<T>(a, kernel, out, max_val, mode, term_of_line, keys, vals, mask, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax) {
+        e = launch_merge(out, keys, vals, table_capacity, frame_of_term, D * H * W,
+                         mode == 4 + kAccSumMax, st, s);
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return CBC_OK;
+}
+
+template <typename T>
+int draw3_impl(T *out, long long n_frames, long long D, long long H, long long W, const T *lines,
+               long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel,
+               int overlap, void *workspace, size_t ws_bytes, long long ck_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || D < 0 || H < 0 || W < 0 || n_lines < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (kernel < CBC_BIWEIGHT || kernel > CBC_TRIANGULAR)
+        return fail(CBC_ERR_INVALID, "kernel is missing");
+    if (overlap != CBC_SUM && overlap != CBC_MAX) return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if (idxs && idx_bytes != 4 && idx_bytes != 8) return fail(CBC_ERR_INVALID, "idx_bytes must be 4 or 8");
+    if (!idxs && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
+        return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
+                                         " != " + std::to_string(n_frames) + ")");
+    if (n_lines > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines");
+    if (D * H * W > INT_MAX) return fail(CBC_ERR_INVALID, "volumes larger than 2^31 voxels");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
+    const long long voxels = n_frames * D * H * W;
+    if (n_lines > 0 && voxels > 0 && (!out || !lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    const Layout3 L = layout3(n_lines, 0, ck_capacity, 0, sizeof(T));
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    init_status_kernel<<<1, 1, 0, s>>>(reinterpret_cast<DevStatus *>(ws + L.status),
+                                       CBC_STRATEGY_LINES);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines == 0 || voxels == 0) return CBC_OK;
+    return run3<T>(out, n_frames, D, H, W, lines, n_lines, idxs, idx_bytes, max_val, kernel,
+                   overlap == CBC_MAX ? 1 : 0, ws, L, ck_capacity, 0, nullptr, nullptr, s);
+}
+
+template <typename T>
+int accumulate3_impl(T *out, long long n_frames, long long D, long long H, long long W,
+                     const T *lines, long long n_lines, const void *terms, int term_bytes,
+                     const void *frames, int frame_bytes, long long n_terms, T max_val,
+                     int kernel, int in_overlap, int out_overlap, void *workspace,
+                     size_t ws_bytes, long long ck_capacity, long long table_capacity,
+                     void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || D < 0 || H < 0 || W < 0 || n_lines < 0 || n_terms < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (kernel < CBC_BIWEIGHT || kernel > CBC_TRIANGULAR)
+        return fail(CBC_ERR_INVALID, "kernel is missing");
+    if ((in_overlap != CBC_SUM && in_overlap != CBC_MAX) ||
+        (out_overlap != CBC_SUM && out_overlap != CBC_MAX))
+        return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if ((term_bytes != 4 && term_bytes != 8) || (frame_bytes != 4 && frame_bytes != 8))
+        return fail(CBC_ERR_INVALID, "term_bytes and frame_bytes must be 4 or 8");
+    if (n_lines > 0 && (!terms || !lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_terms > 0 && !frames) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_lines > INT_MAX || n_terms > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines or terms");
+    if (D * H * W > INT_MAX) return fail(CBC_ERR_INVALID, "volumes larger than 2^31 voxels");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
+    const int acc = (in_overlap == CBC_MAX ? 1 : 0) | (out_overlap == CBC_MAX ? 2 : 0);
+    const bool table = acc == kAccMaxSum || acc == kAccSumMax;
+    if (table && (table_capacity < 1 || (table_capacity & (table_capacity - 1))))
+        return fail(CBC_ERR_INVALID, "table_capacity must be a power of two");
+    if (!table) table_capacity = 0;
+    const long long voxels = n_frames * D * H * W;
+    if (n_lines > 0 && voxels > 0 && !out) return fail(CBC_ERR_INVALID, "null pointer");
+    const Layout3 L = layout3(n_lines, n_terms, ck_capacity, table_capacity, sizeof(T));
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    int *frame_of_line = reinterpret_cast<int *>(ws + L.frame_of_line);
+    int *term_of_line = reinterpret_cast<int *>(ws + L.term_of_line);
+    int *frame_of_term = reinterpret_cast<int *>(ws + L.frame_of_term);
+    init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = launch_frames_check(frames, frame_bytes, n_terms, n_frames, frame_of_term, st, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines == 0 || voxels == 0) return CBC_OK;
+    e = launch_term_frames(terms, term_bytes, frame_of_term, n_lines, n_terms, term_of_line,
+                           frame_of_line, st, s);
+    if (e == cudaSuccess && table)
+        e = clear_table(reinterpret_cast<unsigned long long *>(ws + L.keys),
+                        reinterpret_cast<T *>(ws + L.vals), table_capacity, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return run3<T>(out, n_frames, D, H, W, lines, n_lines, frame_of_line, 4, max_val, kernel,
+                   4 + acc, ws, L, ck_capacity, table_capacity, term_of_line, frame_of_term, s);
+}
+
+}  // namespace l3
+}  // namespace cbc
+
+extern "C" {
+
+size_t cbc_draw_lines_3d_workspace_size(int64_t n_lines, int64_t checkpoint_capacity,
+                                        int32_t elem_bytes)
+{
+    if (n_lines < 0 || checkpoint_capacity < 0 || (elem_bytes != 4 && elem_bytes != 8)) return 0;
+    return cbc::l3::layout3(n_lines, 0, checkpoint_capacity, 0, (size_t)elem_bytes).total;
+}
+
+int cbc_draw_lines_3d_f32(float *out, int64_t n_frames, int64_t depth, int64_t height,
+                          int64_t width, const float *lines, int64_t n_lines, const void *idxs,
+                          int32_t idx_bytes, float max_val, int32_t kernel, int32_t overlap,
+                          void *workspace, size_t workspace_bytes, int64_t checkpoint_capacity,
+                          void *stream)
+{
+    return cbc::l3::draw3_impl<float>(out, n_frames, depth, height, width, lines, n_lines, idxs,
+                                      idx_bytes, max_val, kernel, overlap, workspace,
+                                      workspace_bytes, checkpoint_capacity, stream);
+}
+
+int cbc_draw_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, int64_t height,
+                          int64_t width, const double *lines, int64_t n_lines, const void *idxs,
+                          int32_t idx_bytes, double max_val, int32_t kernel, int32_t overlap,
+                          void *workspace, size_t workspace_bytes, int64_t checkpoint_capacity,
+                          void *stream)
+{
+    return cbc::l3::draw3_impl<double>(out, n_frames, depth, height, width, lines, n_lines, idxs,
+                                       idx_bytes, max_val, kernel, overlap, workspace,
+                                       workspace_bytes, checkpoint_capacity, stream);
+}
+
+size_t cbc_accumulate_lines_3d_workspace_size(int64_t n_lines, int64_t n_terms,
+                                              int64_t checkpoint_capacity,
+                                              int64_t table_capacity, int32_t elem_bytes)
+{
+    if (n_lines < 0 || n_terms < 0 || checkpoint_capacity < 0 || table_capacity < 0 ||
+        (elem_bytes != 4 && elem_bytes != 8))
+        return 0;
+    return cbc::l3::layout3(n_lines, n_terms, checkpoint_capacity, table_capacity,
+                            (size_t)elem_bytes).total;
+}
+
+int cbc_accumulate_lines_3d_f32(float *out, int64_t n_frames, int64_t depth, int64_t height,
+                                int64_t width, const float *lines, int64_t n_lines,
+                                const void *terms, int32_t term_bytes, const void *frames,
+                                int32_t frame_bytes, int64_t n_terms, float max_val,
+                                int32_t kernel, int32_t in_overlap, int32_t out_overlap,
+                                void *workspace, size_t workspace_bytes,
+                                int64_t checkpoint_capacity, int64_t table_capacity, void *stream)
+{
+    return cbc::l3::accumulate3_impl<float>(out, n_frames, depth, height, width, lines, n_lines,
+                                            terms, term_bytes, frames, frame_bytes, n_terms,
+                                            max_val, kernel, in_overlap, out_overlap, workspace,
+                                            workspace_bytes, checkpoint_capacity, table_capacity,
+                                            stream);
+}
+
+int cbc_accumulate_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, int64_t height,
+                                int64_t width, const double *lines, int64_t n_lines,
+                                const void *terms, int32_t term_bytes, const void *frames,
+                                int32_t frame_bytes, int64_t n_terms, double max_val,
+                                int32_t kernel, int32_t in_overlap, int32_t out_overlap,
+                                void *workspace, size_t workspace_bytes,
+                                int64_t checkpoint_capacity, int64_t table_capacity, void *stream)
+{
+    return cbc::l3::accumulate3_impl<double>(out, n_frames, depth, height, width, lines, n_lines,
+                                             terms, term_bytes, frames, frame_bytes, n_terms,
+                                             max_val, kernel, in_overlap, out_overlap, workspace,
+                                             workspace_bytes, checkpoint_capacity,
+                                             table_capacity, stream);
+}
+
+}  // extern "C"

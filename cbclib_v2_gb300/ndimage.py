@@ -87,9 +87,76 @@ def _as_device_lines(lines, dev: torch.device, dtype: torch.dtype) -> torch.Tens
     L = t.shape[-1]
     if L not in (5, 7):
         raise RuntimeError(f"Invalid lines size ({L}) at axis {t.ndim - 1}")
-    if L == 7:
-        raise NotImplementedError("3-D lines are not supported by the GPU path yet")
     return t.to(device=dev, dtype=dtype).reshape(-1, L).contiguous()
+
+
+def _volumes_of(out: torch.Tensor):
+    """(F, D, H, W) of an output for 3-D lines"""
+    if out.dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"out must be float32 or float64, got {out.dtype}")
+    if out.dim() < 3:
+        raise ValueError(f"Output array dimensions ({out.dim()}) do not match the line size (7)")
+    D, H, W = (int(s) for s in out.shape[-3:])
+    return math.prod(int(s) for s in out.shape[:-3]), D, H, W
+
+
+def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
+          table_cap: int = 0, on_status=None) -> None:
+    """Run a 3-D library call ``call(buf, ck_capacity, table_capacity, stream)`` with
+    this thread's workspace, raise the status' errors and retry with more room when the
+    call reports that its checkpoints or its table did not fit."""
+    lib = _native.lib()
+    with torch.cuda.device(dev):
+        stream = torch.cuda.current_stream(dev)
+        key = (kind, dev.index, stream.cuda_stream, threading.get_ident())
+        with _ws_lock:
+            ws = _workspaces.setdefault(key, Workspace(dev))
+        ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
+        table_cap = max(ws.capacity, table_cap) if table_cap else 0
+        for _ in range(6):
+            buf = ws.ensure(size(ck_capacity, table_cap))
+            rc = call(buf, ck_capacity, table_cap, stream.cuda_stream)
+            if rc:
+                _raise_rc(rc)
+            st = _native.Status()
+            if lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream):
+                _raise_rc(_native.CBC_ERR_CUDA)
+            ws.last_status = st
+            if on_status is not None:
+                on_status(st)
+            _raise_status(st, n_frames)
+            if not st.has(_native.CBC_ERR_CAPACITY):
+                ws.ck_capacity = ck_capacity
+                ws.capacity = table_cap
+                return
+            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
+            if table_cap:
+                table_cap = max(table_cap, int(st.pairs_needed))
+            if ck_capacity > 2**31 - 1:
+                raise MemoryError("too many walk checkpoints for one call")
+    raise RuntimeError("workspace capacity did not converge")
+
+
+def _draw_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, idxs, max_val: float, kernel: int,
+                       overlap: int) -> torch.Tensor:
+    F, D, H, W = _volumes_of(out)
+    n_lines = ln.shape[0]
+    ix = _as_device_idxs(idxs, n_lines, out.device)
+    if ix is None and n_lines and F != 1 and F != n_lines:
+        raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
+    work = out if out.is_contiguous() else out.contiguous()
+    elem = 4 if out.dtype == torch.float32 else 8
+    lib = _native.lib()
+    fn = lib.cbc_draw_lines_3d_f32 if elem == 4 else lib.cbc_draw_lines_3d_f64
+    _run3(lambda buf, ck, _t, stream: fn(
+              work.data_ptr(), F, D, H, W, ln.data_ptr(), n_lines,
+              None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+              max_val, kernel, overlap, buf.data_ptr(), buf.numel(), ck, stream),
+          lambda ck, _t: lib.cbc_draw_lines_3d_workspace_size(n_lines, ck, elem),
+          out.device, 'draw3d', F, n_lines)
+    if work is not out:
+        out.copy_(work)
+    return out
 
 
 def _as_device_idxs(idxs, n_lines: int, dev: torch.device) -> Optional[torch.Tensor]:
@@ -193,9 +260,11 @@ def _frames_of(out: torch.Tensor):
 
 def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int,
                      overlap: int, tuning: Optional[_native.Tuning] = None) -> torch.Tensor:
+    ln = _as_device_lines(lines, out.device, out.dtype)
+    if ln.shape[1] == 7:
+        return _draw_lines3d_cuda(out, ln, idxs, max_val, kernel, overlap)
     F, H, W = _frames_of(out)
     dev = out.device
-    ln = _as_device_lines(lines, dev, out.dtype)
     n_lines = ln.shape[0]
     ix = _as_device_idxs(idxs, n_lines, dev)
     if ix is None and n_lines and F != 1 and F != n_lines:
@@ -228,6 +297,8 @@ def draw_lines_csr(out: torch.Tensor, lines, frame_offsets, max_val: float = 1.0
     F, H, W = _frames_of(out)
     dev = out.device
     ln = _as_device_lines(lines, dev, out.dtype)
+    if ln.shape[1] != 5:
+        raise ValueError("draw_lines_csr takes 2-D lines (N, 5)")
     n_lines = ln.shape[0]
     offs = torch.as_tensor(frame_offsets).to(device=dev, dtype=torch.int64).reshape(-1)
     if offs.numel() != F + 1:
@@ -337,9 +408,11 @@ def _table_capacity(ln: torch.Tensor) -> int:
 
 def _accumulate_lines_cuda(out: torch.Tensor, lines, terms, frames, max_val: float, kernel: int,
                            in_ov: int, out_ov: int) -> torch.Tensor:
-    F, H, W = _frames_of(out)
     dev = out.device
     ln = _as_device_lines(lines, dev, out.dtype)
+    if ln.shape[1] == 7:
+        return _accumulate_lines3d_cuda(out, ln, terms, frames, max_val, kernel, in_ov, out_ov)
+    F, H, W = _frames_of(out)
     n_lines = ln.shape[0]
     tm = _as_device_ints(terms, 'terms', dev)
     if tm.numel() != n_lines:
@@ -394,6 +467,52 @@ def _accumulate_lines_cuda(out: torch.Tensor, lines, terms, frames, max_val: flo
     if work is not out:
         out.copy_(work)
     return out
+
+
+def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames, max_val: float,
+                             kernel: int, in_ov: int, out_ov: int) -> torch.Tensor:
+    F, D, H, W = _volumes_of(out)
+    dev = out.device
+    n_lines = ln.shape[0]
+    tm = _as_device_ints(terms, 'terms', dev)
+    if tm.numel() != n_lines:
+        raise ValueError(f"Term indices ({tm.numel()}) is incompatible with number of lines "
+                         f"({n_lines})")
+    fr = _as_device_ints(frames, 'frames', dev)
+    n_terms = fr.numel()
+    work = out if out.is_contiguous() else out.contiguous()
+    elem = 4 if out.dtype == torch.float32 else 8
+    lib = _native.lib()
+    fn = lib.cbc_accumulate_lines_3d_f32 if elem == 4 else lib.cbc_accumulate_lines_3d_f64
+    table = in_ov != out_ov
+    cap = _table_capacity3(ln) if (table and n_lines) else 0
+
+    def check(st):
+        if st.has(_native.CBC_ERR_INDEX):
+            raise IndexError(f"frames range ({int(fr.min())}, {int(fr.max())}) is outside of "
+                             f"(0, {F})")
+        if st.has(_native.CBC_ERR_TERM):
+            raise IndexError(f"Term index {int(tm[st.bad_line])} is out of range (0, {n_terms})")
+
+    _run3(lambda buf, ck, t, stream: fn(
+              work.data_ptr(), F, D, H, W, ln.data_ptr(), n_lines, tm.data_ptr(),
+              tm.element_size(), fr.data_ptr(), fr.element_size(), n_terms, max_val, kernel,
+              in_ov, out_ov, buf.data_ptr(), buf.numel(), ck, t, stream),
+          lambda ck, t: lib.cbc_accumulate_lines_3d_workspace_size(n_lines, n_terms, ck, t, elem),
+          dev, 'accumulate3d', F, n_lines, cap, check)
+    if work is not out:
+        out.copy_(work)
+    return out
+
+
+def _table_capacity3(ln: torch.Tensor) -> int:
+    """the 3-D analogue of _table_capacity: (long extent + 2w + 3) columns of
+    (3w + 2)^2 voxels"""
+    d = (ln[:, 3:6] - ln[:, 0:3]).abs()
+    w = ln[:, 6].clamp(min=0)
+    est = float(((d.max(dim=1).values + 2 * w + 3) * (3 * w + 2) ** 2).sum().item())
+    need = max(1024, int(2 * est))
+    return 1 << (need - 1).bit_length()
 
 
 def accumulate_lines(out, lines, terms, frames, max_val: float = 1.0,

@@ -236,6 +236,60 @@ CBC_API int cbc_accumulate_lines_f64(double *out, int64_t n_frames, int64_t heig
                                      int64_t checkpoint_capacity, int64_t table_capacity,
                                      void *stream);
 
+/* draw_lines for 3-D lines into volumes.  Replaces the N = 3 instantiations of
+ * bresenham.draw_lines (_src/src/bresenham.cpp:38-101 with draw_line_3d,
+ * bresenham.hpp:389-430; dispatch on the line size :126-139) and of
+ * cuda_draw_lines.draw_lines (_src/src/cuda_draw_lines.cu:925-933).
+ * out: (n_frames, depth, height, width); lines: (n_lines, 7) rows
+ * [x0, y0, z0, x1, y1, z1, width] (xyz order, z the slowest axis of a volume); idxs,
+ * max_val, kernel, overlap and the status as for cbc_draw_lines_f32 (only the
+ * checkpoint capacity applies; pairs_needed stays 0).  A voxel the reference's walk
+ * visits twice is combined twice, as in the reference. */
+CBC_API size_t cbc_draw_lines_3d_workspace_size(int64_t n_lines, int64_t checkpoint_capacity,
+                                                int32_t elem_bytes);
+
+CBC_API int cbc_draw_lines_3d_f32(float *out, int64_t n_frames, int64_t depth, int64_t height,
+                                  int64_t width, const float *lines, int64_t n_lines,
+                                  const void *idxs, int32_t idx_bytes, float max_val,
+                                  int32_t kernel, int32_t overlap, void *workspace,
+                                  size_t workspace_bytes, int64_t checkpoint_capacity,
+                                  void *stream);
+
+CBC_API int cbc_draw_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, int64_t height,
+                                  int64_t width, const double *lines, int64_t n_lines,
+                                  const void *idxs, int32_t idx_bytes, double max_val,
+                                  int32_t kernel, int32_t overlap, void *workspace,
+                                  size_t workspace_bytes, int64_t checkpoint_capacity,
+                                  void *stream);
+
+/* accumulate_lines for 3-D lines into volumes (N = 3 of bresenham.cpp:151-259;
+ * cuda_draw_lines.cu:1034-1042), with the arguments and status of
+ * cbc_accumulate_lines_f32 plus the volume depth. */
+CBC_API size_t cbc_accumulate_lines_3d_workspace_size(int64_t n_lines, int64_t n_terms,
+                                                      int64_t checkpoint_capacity,
+                                                      int64_t table_capacity,
+                                                      int32_t elem_bytes);
+
+CBC_API int cbc_accumulate_lines_3d_f32(float *out, int64_t n_frames, int64_t depth,
+                                        int64_t height, int64_t width, const float *lines,
+                                        int64_t n_lines, const void *terms, int32_t term_bytes,
+                                        const void *frames, int32_t frame_bytes,
+                                        int64_t n_terms, float max_val, int32_t kernel,
+                                        int32_t in_overlap, int32_t out_overlap,
+                                        void *workspace, size_t workspace_bytes,
+                                        int64_t checkpoint_capacity, int64_t table_capacity,
+                                        void *stream);
+
+CBC_API int cbc_accumulate_lines_3d_f64(double *out, int64_t n_frames, int64_t depth,
+                                        int64_t height, int64_t width, const double *lines,
+                                        int64_t n_lines, const void *terms, int32_t term_bytes,
+                                        const void *frames, int32_t frame_bytes,
+                                        int64_t n_terms, double max_val, int32_t kernel,
+                                        int32_t in_overlap, int32_t out_overlap,
+                                        void *workspace, size_t workspace_bytes,
+                                        int64_t checkpoint_capacity, int64_t table_capacity,
+                                        void *stream);
+
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
 CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
