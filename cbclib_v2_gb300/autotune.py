@@ -39,14 +39,26 @@ def candidates() -> List[_native.Tuning]:
             T(32, 32, 16, 128, TI, 0), T(128, 64, 8, 256, TI, 0), T(128, 32, 16, 256, TI, 0)]
 
 
+_names: Dict[int, str] = {}
+
+
+def _device_name(device: Optional[torch.device]) -> str:
+    if not torch.cuda.is_available():
+        return 'cpu'
+    idx = torch.cuda.current_device() if device is None or device.index is None else device.index
+    name = _names.get(idx)
+    if name is None:
+        name = _names[idx] = torch.cuda.get_device_name(idx)
+    return name
+
+
 def workload_key(shape, dtype: torch.dtype, kernel: str, overlap: str, n_lines: int,
                  device: Optional[torch.device] = None) -> str:
     H, W = int(shape[-2]), int(shape[-1])
     F = math.prod(int(s) for s in shape[:-2])
     mpx = max(F * H * W / 1e6, 1e-6)
     bucket = int(math.floor(math.log2(max(n_lines / mpx, 1.0))))
-    name = torch.cuda.get_device_name(device) if torch.cuda.is_available() else 'cpu'
-    return f"{name}|{H}x{W}|{str(dtype).split('.')[-1]}|{kernel}|{overlap}|d{bucket}"
+    return f"{_device_name(device)}|{H}x{W}|{str(dtype).split('.')[-1]}|{kernel}|{overlap}|d{bucket}"
 
 
 def _load():
@@ -79,6 +91,13 @@ def lookup(key: str) -> Optional[_native.Tuning]:
         _load()
         v = _mem.get(key)
     return None if v is None else _native.Tuning(*v)
+
+
+def has_entries() -> bool:
+    """whether any workload class has a cached choice (lets callers skip the key)"""
+    with _lock:
+        _load()
+        return bool(_mem)
 
 
 def _time_call(fn, repeats: int) -> float:

@@ -176,7 +176,7 @@ int accumulate_impl(T *out, long long n_frames, long long H, long long W, const 
     LineRec<T> *recs = reinterpret_cast<LineRec<T> *>(ws + L.recs);
     Checkpoint<T> *cks = reinterpret_cast<Checkpoint<T> *>(ws + L.cks);
     prep_kernel<T, int32_t, false, true><<<nb, kThreads, 0, s>>>(
-        lines, frame_of_line, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st);
+        lines, frame_of_line, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st, nullptr);
     note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));

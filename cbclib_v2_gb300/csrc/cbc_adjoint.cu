@@ -253,10 +253,12 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     const unsigned nb = (unsigned)((n_lines + 255) / 256);
     if (idxs && idx_bytes == 8)
         prep_kernel<T, int64_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                                recs, nullptr, cks, ck_capacity, st);
+                                                                recs, nullptr, cks, ck_capacity, st,
+                                                                nullptr);
     else
         prep_kernel<T, int32_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                                recs, nullptr, cks, ck_capacity, st);
+                                                                recs, nullptr, cks, ck_capacity, st,
+                                                                nullptr);
     note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));

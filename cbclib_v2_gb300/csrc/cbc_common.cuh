@@ -71,6 +71,7 @@ struct DevStatus {
     unsigned long long pairs;      /* running pair cursor == pairs_needed */
     unsigned long long cks;        /* running checkpoint cursor            */
     unsigned long long work;       /* work-item counter of the lines render */
+    unsigned long long nlong;      /* lines in the long-walk list of prep_kernel */
 };
 
 /* per line of the current render chunk */
@@ -415,19 +416,30 @@ __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> 
 
 /* COUNT_TILES: count the line's (frame, tile) bins (tiles strategy); WALK: also write
  * its walk checkpoints here (lines strategy, which needs no bins) */
+/* walks longer than this many columns go to the long-walk list, which
+ * walk_ordered_kernel starts first */
+constexpr int kLongCols = 96;
+
+/* COUNT_TILES: count the line's (frame, tile) bins (tiles strategy); WALK: also write
+ * its walk checkpoints here.  With `longs`, lines longer than kLongCols columns are
+ * listed there instead of walked (walk_ordered_kernel walks everything later).  The
+ * checkpoint cursor, the long list and the index range take one atomic per block. */
 template <typename T, typename IdxT, bool COUNT_TILES, bool WALK>
 __global__ void __launch_bounds__(kThreads)
 prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long long n_lines,
             long long n_frames, Geometry g, LineRec<T> *__restrict__ recs,
             int *__restrict__ counts, Checkpoint<T> *__restrict__ cks, long long ck_capacity,
-            DevStatus *st)
+            DevStatus *st, int *__restrict__ longs)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ unsigned long long s_ck[kThreads / 32];
+    __shared__ int s_long[kThreads / 32];
+    __shared__ long long s_min[kThreads / 32], s_max[kThreads / 32];
+    __shared__ unsigned long long s_ck_base, s_long_base;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = i < n_lines;
     long long frame = 0;
     const bool has_idx = idxs != nullptr;
     if (in) frame = has_idx ? load_idx<IdxT>(idxs, i) : (n_frames == 1 ? 0 : i);
-    if (has_idx) warp_minmax(frame, in, st);
     LineRec<T> r;
     r.flags = 0;
     int nck = 0;
@@ -456,19 +468,52 @@ prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lon
             }
         }
     }
-    /* checkpoint blocks: one atomic per warp on the checkpoint cursor */
-    const int lane = threadIdx.x & 31;
+    const bool is_long = longs != nullptr && (r.flags & kDrawable) && r.ncols > kLongCols;
+    /* warp, then block aggregates */
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int incl = nck;
     for (int o = 1; o < 32; o <<= 1) {
-        int u = __shfl_up_sync(0xffffffffu, incl, o);
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += u;
     }
-    unsigned long long wbase = 0;
-    if (lane == 31) wbase = atomicAdd(&st->cks, (unsigned long long)incl);
-    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    long long mn = (in && has_idx) ? frame : LLONG_MAX, mx = (in && has_idx) ? frame : LLONG_MIN;
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    const unsigned lm = __ballot_sync(0xffffffffu, is_long);
+    if (lane == 31) s_ck[wid] = (unsigned long long)incl;
+    if (lane == 0) {
+        s_long[wid] = __popc(lm);
+        s_min[wid] = mn;
+        s_max[wid] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long c = 0;
+        int l = 0;
+        long long bmn = LLONG_MAX, bmx = LLONG_MIN;
+        for (int w = 0; w < kThreads / 32; w++) {
+            const unsigned long long tc = s_ck[w];
+            s_ck[w] = c;
+            c += tc;
+            const int tl = s_long[w];
+            s_long[w] = l;
+            l += tl;
+            bmn = min(bmn, s_min[w]);
+            bmx = max(bmx, s_max[w]);
+        }
+        s_ck_base = c ? atomicAdd(&st->cks, c) : 0ull;
+        s_long_base = l ? atomicAdd(&st->nlong, (unsigned long long)l) : 0ull;
+        if (bmn <= bmx) {
+            atomicMin(&st->idx_min, bmn);
+            atomicMax(&st->idx_max, bmx);
+        }
+    }
+    __syncthreads();
     if (!in) return;
     if (r.flags & kDrawable) {
-        unsigned long long cb = wbase + (unsigned long long)(incl - nck);
+        const unsigned long long cb = s_ck_base + s_ck[wid] + (unsigned long long)(incl - nck);
         const bool ck_ok = cb + (unsigned long long)nck <= (unsigned long long)ck_capacity;
         if (!ck_ok) {
             atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
@@ -484,7 +529,11 @@ prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lon
                 for (int tj = j0; tj <= j1; tj++) atomicAdd(fc + cv.bin(ti, tj, g), 1);
             }
         }
-        if (WALK && ck_ok) write_checkpoints(r, (int)i, cv, cks, st);
+        if (is_long)
+            longs[s_long_base + (unsigned long long)(s_long[wid] + __popc(lm & ((1u << lane) - 1u)))] =
+                (int)i;
+        else if (WALK && ck_ok)
+            write_checkpoints(r, (int)i, cv, cks, st);
     }
     recs[i] = r;
 }
@@ -499,6 +548,7 @@ static __global__ void init_status_kernel(DevStatus *st, int strategy)
     st->pairs = 0;
     st->cks = 0;
     st->work = 0;
+    st->nlong = 0;
 }
 
 /* bin offsets: block-local exclusive scan + one atomic per block on the pair cursor */
@@ -615,17 +665,28 @@ fill_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
     write_checkpoints(r, (int)i, cv, cks, st);
 }
 
-/* lines strategy: one thread per line writes its walk checkpoints */
+/* the walks prep_kernel listed as long (thread t < nlong, started first so that the
+ * longest sequential walks overlap everything else), then the remaining lines in
+ * index order: one thread per line writes its walk checkpoints */
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-walk_kernel(const LineRec<T> *__restrict__ recs, long long n_lines, Geometry g,
-            Checkpoint<T> *__restrict__ cks, DevStatus *st)
+walk_ordered_kernel(const LineRec<T> *__restrict__ recs, long long n_lines,
+                    const int *__restrict__ longs, Geometry g, Checkpoint<T> *__restrict__ cks,
+                    DevStatus *st)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_lines) return;
     if (st->flags & kFatal) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nlong = (long long)st->nlong;
+    long long i = t;
+    if (t < nlong) {
+        i = longs[t];
+    } else {
+        i = t - nlong;
+        if (i >= n_lines) return;
+    }
     const LineRec<T> r = recs[i];
     if (!(r.flags & kDrawable)) return;
+    if (t >= nlong && r.ncols > kLongCols) return;       /* walked by the first threads */
     Coverage<T> cv;
     if (!cv.init(r, g)) return;
     write_checkpoints(r, (int)i, cv, cks, st);

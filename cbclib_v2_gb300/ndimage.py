@@ -51,6 +51,8 @@ class Workspace:
         self.capacity = 0
         self.ck_capacity = 0
         self.last_status: Optional[_native.Status] = None
+        self.size_key = None             # arguments and result of the last size query
+        self.size_bytes = 0
 
     def ensure(self, nbytes: int) -> torch.Tensor:
         if self.buffer is None or self.buffer.numel() < nbytes:
@@ -64,12 +66,16 @@ _workspaces = {}
 
 
 def _workspace(dev: torch.device, stream: torch.cuda.Stream) -> Workspace:
-    key = (dev.index, stream.cuda_stream, threading.get_ident())
-    with _ws_lock:
-        ws = _workspaces.get(key)
-        if ws is None:
-            ws = _workspaces[key] = Workspace(dev)
-        return ws
+    return _workspace_raw(dev, stream.cuda_stream)
+
+
+def _workspace_raw(dev: torch.device, stream: int) -> Workspace:
+    key = (dev.index, stream, threading.get_ident())
+    ws = _workspaces.get(key)           # dict reads are atomic; creation takes the lock
+    if ws is None:
+        with _ws_lock:
+            ws = _workspaces.setdefault(key, Workspace(dev))
+    return ws
 
 
 def _check_names(kernel: str, overlap: str) -> Tuple[int, int]:
@@ -195,11 +201,39 @@ def _resolve_tuning(tuning, out: torch.Tensor, n_lines: int, kernel: int, overla
         tuning = getattr(_tls, 'tuning', None)
     if tuning is None:
         from . import autotune
-        names = {v: k for k, v in _native.KERNELS.items()}
-        ovn = {v: k for k, v in _native.OVERLAPS.items()}
-        tuning = autotune.lookup(autotune.workload_key(out.shape, out.dtype, names[kernel],
-                                                       ovn[overlap], n_lines, out.device))
+        if autotune.has_entries():
+            tuning = autotune.lookup(autotune.workload_key(
+                out.shape, out.dtype, _KERNEL_NAMES[kernel], _OVERLAP_NAMES[overlap], n_lines,
+                out.device))
     return tuning
+
+
+_KERNEL_NAMES = {v: k for k, v in _native.KERNELS.items()}
+_OVERLAP_NAMES = {v: k for k, v in _native.OVERLAPS.items()}
+
+
+def _current_stream(dev: torch.device) -> int:
+    """raw handle of the current stream of `dev`"""
+    raw = getattr(torch._C, '_cuda_getCurrentRawStream', None)
+    if raw is not None:
+        return raw(dev.index)
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+class _on_current_device:
+    """`with torch.cuda.device(dev)` that costs nothing when `dev` is already current"""
+    def __init__(self, dev: torch.device):
+        self.dev = dev
+        self.ctx = None
+
+    def __enter__(self):
+        if self.dev.index != torch.cuda.current_device():
+            self.ctx = torch.cuda.device(self.dev)
+            self.ctx.__enter__()
+
+    def __exit__(self, *exc):
+        if self.ctx is not None:
+            self.ctx.__exit__(*exc)
 
 
 def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines: int,
@@ -208,23 +242,30 @@ def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines
     workspace, read the status, raise the reference's errors and repeat with a larger
     workspace when the call reports that its pairs or checkpoints did not fit."""
     lib = _native.lib()
-    with torch.cuda.device(dev):
-        stream = torch.cuda.current_stream(dev)
-        ws = _workspace(dev, stream)
+    with _on_current_device(dev):
+        stream = _current_stream(dev)
+        ws = _workspace_raw(dev, stream)
         capacity = max(ws.capacity, 4 * n_lines + 1024)
         ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
         tref = None if tuning is None else ctypes_pointer(tuning)
         for _ in range(4):
-            nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity, ck_capacity,
-                                                       elem, tref)
-            if nbytes == 0:
-                raise ValueError(_native.last_error() or "invalid sizes or tuning")
+            size_key = (F, H, W, n_lines, capacity, ck_capacity, elem,
+                        None if tuning is None else tuple(getattr(tuning, f) for f, _ in
+                                                          _native.Tuning._fields_))
+            if ws.size_key == size_key:
+                nbytes = ws.size_bytes
+            else:
+                nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity,
+                                                           ck_capacity, elem, tref)
+                if nbytes == 0:
+                    raise ValueError(_native.last_error() or "invalid sizes or tuning")
+                ws.size_key, ws.size_bytes = size_key, nbytes
             buf = ws.ensure(nbytes)
-            rc = call(buf, capacity, ck_capacity, tref, stream.cuda_stream)
+            rc = call(buf, capacity, ck_capacity, tref, stream)
             if rc:
                 _raise_rc(rc)
             st = _native.Status()
-            rc = lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream)
+            rc = lib.cbc_read_status(buf.data_ptr(), st, stream)
             if rc:
                 _raise_rc(rc)
             ws.last_status = st

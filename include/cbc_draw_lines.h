@@ -54,7 +54,7 @@ extern "C" {
 #define CBC_MAX 1
 
 /* render strategies */
-#define CBC_STRATEGY_AUTO  0   /* pick by line density                                  */
+#define CBC_STRATEGY_AUTO  0   /* the library's choice: the lines strategy            */
 #define CBC_STRATEGY_TILES 1   /* (frame, tile) bins, shared-memory tiles, one pass out */
 #define CBC_STRATEGY_LINES 2   /* warps of 32 lines, L2 reductions into out             */
 
