@@ -226,7 +226,7 @@ def run_fit(args, world, rank, local):
     cost of a finite-difference gradient from the plain forward (2 forwards per
     parameter, 5 parameters per line)"""
     import torch
-    from cbclib_v2_gb300 import _native, autograd, draw_lines, workloads
+    from cbclib_v2_gb300 import _native, autograd, draw_lines, fit, workloads
     torch.cuda.set_device(local)
     ls = workloads.fit_stack(seed=2000 + rank)
     truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
@@ -246,17 +246,28 @@ def run_fit(args, world, rank, local):
         loss.backward()
         return loss
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    image = torch.empty_like(target)
+
+    def fused_step():
+        return fit.squared_loss_step(image, target, truth, idxs, ls.max_val, ls.kernel,
+                                     ls.overlap)
+
     stream = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(args.steps):
-        loss = step()
-    b.record(stream)
-    torch.cuda.synchronize()
-    ms_iter = a.elapsed_time(b) / args.steps
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(args.steps):
+            r = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / args.steps, r
+
+    ms_iter, _ = timed(fused_step)                 # forward + fused loss adjoint
+    ms_autograd, loss = timed(step)                # torch autograd and a torch loss
     # one plain forward, the unit of a finite-difference gradient
     out = torch.zeros(ls.shape, device='cuda')
     for _ in range(3):
@@ -280,6 +291,8 @@ def run_fit(args, world, rank, local):
             'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
                        'kernel': ls.kernel, 'overlap': ls.overlap,
                        'loss': 'sum((I - target)^2), target = Poisson(render(perturbed))'},
+            'path': 'fused: draw_lines + squared-loss adjoint (2 (I - T) per drawn pixel)',
+            'autograd_ms_per_iter': ms_autograd,
             'forward_ms': ms_fwd,
             'finite_difference_gradient_ms': fd_ms,
             'speedup_vs_finite_difference': fd_ms / ms_iter,

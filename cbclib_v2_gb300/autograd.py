@@ -16,19 +16,85 @@ import torch
 
 from . import _native, ndimage
 
-__all__ = ['draw_lines_fn', 'DrawLinesFunction', 'lines_backward']
+__all__ = ['draw_lines_fn', 'DrawLinesFunction', 'lines_backward', 'squared_loss_backward']
 
 _ws_lock = threading.Lock()
 _workspaces = {}
 
 
-def _workspace(dev: torch.device, stream) -> ndimage.Workspace:
-    key = ('adjoint', dev.index, stream.cuda_stream, threading.get_ident())
-    with _ws_lock:
+def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dtype, dev,
+              grad_out: Optional[torch.Tensor] = None, image: Optional[torch.Tensor] = None,
+              out0: Optional[torch.Tensor] = None, winner: Optional[torch.Tensor] = None,
+              target: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """One adjoint call: with grad_out, cbc_draw_lines_backward_*; with target instead,
+    cbc_squared_loss_backward_* (grad_out = 2 (image - target) formed per pixel)."""
+    k, ov = ndimage._check_names(kernel, overlap)
+    if dtype not in (torch.float32, torch.float64):
+        raise TypeError(f"frames must be float32 or float64, got {dtype}")
+    ln = ndimage._as_device_lines(lines, dev, dtype)
+    if ln.shape[1] != 5:
+        raise ValueError("gradients are implemented for 2-D lines (N, 5)")
+    n = ln.shape[0]
+    ix = ndimage._as_device_idxs(idxs, n, dev)
+    H, W = int(shape[-2]), int(shape[-1])
+    F = math.prod(int(s) for s in shape[:-2])
+    img = None if image is None else image.to(dtype).contiguous()
+    o0 = None if out0 is None else out0.to(dtype).contiguous()
+    if ov == _native.OVERLAPS['max']:
+        if img is None:
+            raise ValueError("max overlap needs the forward image")
+        if winner is None:
+            winner = torch.empty(tuple(shape), dtype=torch.int32, device=dev)
+    grad = torch.empty((n, 5), dtype=dtype, device=dev)
+    lib = _native.lib()
+    elem = 4 if dtype == torch.float32 else 8
+    sfx = 'f32' if elem == 4 else 'f64'
+    if target is None:
+        g = grad_out.contiguous()
+        fn = getattr(lib, 'cbc_draw_lines_backward_' + sfx)
+
+        def call(buf, ck_capacity, stream):
+            return fn(g.data_ptr(), F, H, W, ln.data_ptr(), n,
+                      None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                      max_val, k, ov, None if img is None else img.data_ptr(),
+                      None if o0 is None else o0.data_ptr(),
+                      None if winner is None else winner.data_ptr(), grad.data_ptr(),
+                      buf.data_ptr(), buf.numel(), ck_capacity, stream)
+    else:
+        tg = target.to(dtype).contiguous()
+        if img is None:
+            raise ValueError("the squared loss needs the forward image")
+        fn = getattr(lib, 'cbc_squared_loss_backward_' + sfx)
+
+        def call(buf, ck_capacity, stream):
+            return fn(img.data_ptr(), tg.data_ptr(), F, H, W, ln.data_ptr(), n,
+                      None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                      max_val, k, ov, None if o0 is None else o0.data_ptr(),
+                      None if winner is None else winner.data_ptr(), grad.data_ptr(),
+                      buf.data_ptr(), buf.numel(), ck_capacity, stream)
+    with ndimage._on_current_device(dev):
+        stream = ndimage._current_stream(dev)
+        key = ('adjoint', dev.index, stream, threading.get_ident())
         ws = _workspaces.get(key)
         if ws is None:
-            ws = _workspaces[key] = ndimage.Workspace(dev)
-        return ws
+            with _ws_lock:
+                ws = _workspaces.setdefault(key, ndimage.Workspace(dev))
+        ck_capacity = max(ws.ck_capacity, 16 * n + 1024)
+        for _ in range(4):
+            nbytes = lib.cbc_draw_lines_backward_workspace_size(n, ck_capacity, elem)
+            buf = ws.ensure(nbytes)
+            rc = call(buf, ck_capacity, stream)
+            if rc:
+                ndimage._raise_rc(rc)
+            st = _native.Status()
+            if lib.cbc_read_status(buf.data_ptr(), st, stream):
+                ndimage._raise_rc(_native.CBC_ERR_CUDA)
+            ndimage._raise_status(st, F)
+            if not st.has(_native.CBC_ERR_CAPACITY):
+                ws.ck_capacity = ck_capacity
+                return grad
+            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
+    raise RuntimeError("checkpoint capacity did not converge")
 
 
 def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[torch.Tensor],
@@ -40,67 +106,35 @@ def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[t
     ``grad_out`` has the frames' shape and dtype.  Max overlap also needs the forward
     result ``image`` (and ``out0`` if the frames were not zeros); ``winner`` (int32,
     frames' shape) is filled with each pixel's winning line when given."""
-    k, ov = ndimage._check_names(kernel, overlap)
-    dev, dtype = grad_out.device, grad_out.dtype
-    if dtype not in (torch.float32, torch.float64):
-        raise TypeError(f"grad_out must be float32 or float64, got {dtype}")
-    ln = ndimage._as_device_lines(lines, dev, dtype)
-    if ln.shape[1] != 5:
-        raise ValueError("gradients are implemented for 2-D lines (N, 5)")
-    n = ln.shape[0]
-    ix = ndimage._as_device_idxs(idxs, n, dev)
-    H, W = int(grad_out.shape[-2]), int(grad_out.shape[-1])
-    F = math.prod(int(s) for s in grad_out.shape[:-2])
-    g = grad_out.contiguous()
-    img = o0 = None
-    if ov == _native.OVERLAPS['max']:
-        if image is None:
-            raise ValueError("max overlap needs the forward image")
-        img = image.to(dtype).contiguous()
-        o0 = None if out0 is None else out0.to(dtype).contiguous()
-        if winner is None:
-            winner = torch.empty(grad_out.shape, dtype=torch.int32, device=dev)
-    grad = torch.empty((n, 5), dtype=dtype, device=dev)
-    lib = _native.lib()
-    elem = 4 if dtype == torch.float32 else 8
-    fn = lib.cbc_draw_lines_backward_f32 if elem == 4 else lib.cbc_draw_lines_backward_f64
-    with torch.cuda.device(dev):
-        stream = torch.cuda.current_stream(dev)
-        ws = _workspace(dev, stream)
-        ck_capacity = max(ws.ck_capacity, 16 * n + 1024)
-        for _ in range(4):
-            nbytes = lib.cbc_draw_lines_backward_workspace_size(n, ck_capacity, elem)
-            buf = ws.ensure(nbytes)
-            rc = fn(g.data_ptr(), F, H, W, ln.data_ptr(), n,
-                    None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
-                    max_val, k, ov, None if img is None else img.data_ptr(),
-                    None if o0 is None else o0.data_ptr(),
-                    None if winner is None else winner.data_ptr(), grad.data_ptr(),
-                    buf.data_ptr(), buf.numel(), ck_capacity, stream.cuda_stream)
-            if rc:
-                ndimage._raise_rc(rc)
-            st = _native.Status()
-            if lib.cbc_read_status(buf.data_ptr(), st, stream.cuda_stream):
-                ndimage._raise_rc(_native.CBC_ERR_CUDA)
-            ndimage._raise_status(st, F)
-            if not st.has(_native.CBC_ERR_CAPACITY):
-                ws.ck_capacity = ck_capacity
-                return grad
-            ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
-    raise RuntimeError("checkpoint capacity did not converge")
+    return _backward(lines, idxs, max_val, kernel, overlap, grad_out.shape, grad_out.dtype,
+                     grad_out.device, grad_out=grad_out, image=image, out0=out0, winner=winner)
+
+
+def squared_loss_backward(image: torch.Tensor, target: torch.Tensor, lines: torch.Tensor,
+                          idxs: Optional[torch.Tensor], max_val: float, kernel: str,
+                          overlap: str, out0: Optional[torch.Tensor] = None,
+                          winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """(N, 5) gradient of sum((image - target)^2) with respect to ``lines``, where
+    ``image = out0 + draw_lines(lines, ...)`` is the forward result (``out0`` None:
+    zeros).  The adjoint kernels form 2 (image - target) at each drawn pixel, so no
+    full-frame gradient is stored (the fused loss step of a streak fit)."""
+    return _backward(lines, idxs, max_val, kernel, overlap, image.shape, image.dtype,
+                     image.device, image=image, out0=out0, winner=winner, target=target)
 
 
 class DrawLinesFunction(torch.autograd.Function):
     """frames = out0 + draw_lines(lines); gradients for lines and out0."""
 
     @staticmethod
-    def forward(ctx, lines, out0, idxs, max_val, kernel, overlap):
+    def forward(ctx, lines, out0, idxs, max_val, kernel, overlap, zero_base=False):
         image = out0.detach().clone(memory_format=torch.contiguous_format)
         k, ov = ndimage._check_names(kernel, overlap)
         ndimage._draw_lines_cuda(image, lines.detach(), idxs, max_val, k, ov)
         ctx.meta = (max_val, kernel, overlap)
         if overlap == 'max':
-            ctx.save_for_backward(lines.detach(), idxs, image, out0.detach())
+            # frames that started at zero need no out0 in the winner pass
+            ctx.save_for_backward(lines.detach(), idxs, image,
+                                  None if zero_base else out0.detach())
         else:
             ctx.save_for_backward(lines.detach(), idxs)
         return image
@@ -129,7 +163,7 @@ class DrawLinesFunction(torch.autograd.Function):
                 grad_out0 = g
         if grad_lines is not None:
             grad_lines = grad_lines.to(lines.dtype).reshape(lines.shape)
-        return grad_lines, grad_out0, None, None, None, None
+        return grad_lines, grad_out0, None, None, None, None, None
 
 
 def draw_lines_fn(lines: torch.Tensor, idxs: Optional[torch.Tensor] = None, *,
@@ -138,6 +172,7 @@ def draw_lines_fn(lines: torch.Tensor, idxs: Optional[torch.Tensor] = None, *,
                   overlap: str = 'sum') -> torch.Tensor:
     """New frames ``out0 + draw_lines(lines)``, differentiable in ``lines`` (N, 5) and
     ``out0``.  Give either ``shape`` (frames start at zero) or ``out0``."""
+    zero_base = out0 is None
     if out0 is None:
         if shape is None:
             raise ValueError("give shape or out0")
@@ -145,4 +180,4 @@ def draw_lines_fn(lines: torch.Tensor, idxs: Optional[torch.Tensor] = None, *,
     if lines.shape[-1] != 5:
         raise RuntimeError(f"Invalid lines size ({lines.shape[-1]}) at axis {lines.ndim - 1}")
     ndimage._check_names(kernel, overlap)
-    return DrawLinesFunction.apply(lines, out0, idxs, float(max_val), kernel, overlap)
+    return DrawLinesFunction.apply(lines, out0, idxs, float(max_val), kernel, overlap, zero_base)

@@ -41,10 +41,12 @@ struct AccumAct {
     T *vals;
     unsigned long long mask;       /* table capacity - 1 (a power of two) */
     DevStatus *st;
+    struct Pre {};
     __device__ __forceinline__ void item_begin(int) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
+    __device__ __forceinline__ Pre prefetch(const SlotTable<T> &, int, int, int) const { return {}; }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
-                                          T, T) {
+                                          T, T, Pre) {
         using A = Ar<T>;
         const T v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
         const long long pix = (long long)py * W + px;

@@ -38,16 +38,24 @@ struct WinnerAct {
     T max_val;
     int W;
     const float *gtab;   /* gaussian table (shared-memory copy) */
+    struct Pre {
+        T img, o;
+    };
     __device__ __forceinline__ void item_begin(int) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
+    __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
+        const long long at = S.fbase[slot] + (long long)py * W + px;
+        Pre p;
+        p.img = image[at];
+        p.o = out0 ? out0[at] : T(0);
+        return p;
+    }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
-                                          T, T) {
+                                          T, T, const Pre &p) {
         using A = Ar<T>;
         const long long at = S.fbase[slot] + (long long)py * W + px;
         const T v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
-        const T img = image[at];
-        const T o = out0 ? out0[at] : T(0);
-        if (v == img && o < img) atomicMin(winner + at, S.line[slot]);
+        if (v == p.img && p.o < p.img) atomicMin(winner + at, S.line[slot]);
     }
 };
 
@@ -67,7 +75,9 @@ __device__ __forceinline__ T kappa_of(T d, T w, T max_val)
 template <typename T, int K, int OV>
 struct BackwardAct {
     static constexpr bool kNeedsGeometry = true;
-    const T *grad_out;
+    const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
+    const T *image;
+    const T *target;
     const int *winner;   /* max overlap */
     double *gacc;        /* (N, 5) */
     T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
@@ -86,11 +96,21 @@ struct BackwardAct {
             if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
         }
     }
-    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
-                                          T) {
+    struct Pre {
+        int win;
+        T g;
+    };
+    __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
         const long long at = S.fbase[slot] + (long long)py * W + px;
-        if (OV == CBC_MAX && winner[at] != S.line[slot]) return;
-        const T g = grad_out[at];
+        Pre p;
+        p.win = OV == CBC_MAX ? winner[at] : 0;
+        p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
+        return p;
+    }
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
+                                          T, const Pre &p) {
+        if (OV == CBC_MAX && p.win != S.line[slot]) return;
+        const T g = p.g;
         if (g == T(0)) return;
         const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
         const T w = S.w[slot];
@@ -119,6 +139,7 @@ struct AdjArgs {
     const T *grad_out;
     const T *image;
     const T *out0;
+    const T *target;
     int *winner;
     double *gacc;
     T max_val;
@@ -145,6 +166,8 @@ backward_kernel(AdjArgs<T> a)
     __shared__ T acc_s[kSegWarps][32][5];
     BackwardAct<T, K, OV> act;
     act.grad_out = a.grad_out;
+    act.image = a.image;
+    act.target = a.target;
     act.winner = a.winner;
     act.gacc = a.gacc;
     act.acc = acc_s[threadIdx.x >> 5];
@@ -205,7 +228,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
                   const T *lines, long long n_lines, const void *idxs, int idx_bytes,
                   T max_val, int kernel, int overlap, const T *image, const T *out0,
                   int *winner, T *grad_lines, void *workspace, size_t ws_bytes,
-                  long long ck_capacity, void *stream)
+                  long long ck_capacity, void *stream, const T *target = nullptr)
 {
     clear_error();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
@@ -225,7 +248,8 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
     const bool pixels = n_frames * H * W > 0;
     if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
-    if (n_lines > 0 && pixels && !grad_out) return fail(CBC_ERR_INVALID, "null grad_out");
+    if (n_lines > 0 && pixels && !grad_out && !(target && image))
+        return fail(CBC_ERR_INVALID, "null grad_out");
     if (overlap == CBC_MAX && n_lines > 0 && pixels && (!image || !winner))
         return fail(CBC_ERR_INVALID, "max overlap needs the forward image and a winner buffer");
     AdjLayout L = adj_layout(n_lines, ck_capacity, sizeof(LineRec<T>), sizeof(Checkpoint<T>));
@@ -277,6 +301,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.grad_out = grad_out;
         aa.image = image;
         aa.out0 = out0;
+        aa.target = target;
         aa.winner = winner;
         aa.gacc = gacc;
         aa.max_val = max_val;
@@ -336,6 +361,36 @@ int cbc_draw_lines_backward_f64(const double *grad_out, int64_t n_frames, int64_
                                       idx_bytes, max_val, kernel, overlap, image, out0, winner,
                                       grad_lines, workspace, workspace_bytes,
                                       checkpoint_capacity, stream);
+}
+
+int cbc_squared_loss_backward_f32(const float *image, const float *target, int64_t n_frames,
+                                  int64_t height, int64_t width, const float *lines,
+                                  int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                  float max_val, int32_t kernel, int32_t overlap,
+                                  const float *out0, int32_t *winner, float *grad_lines,
+                                  void *workspace, size_t workspace_bytes,
+                                  int64_t checkpoint_capacity, void *stream)
+{
+    if (!image || !target) return cbc::fail(CBC_ERR_INVALID, "null image or target");
+    return cbc::backward_impl<float>(nullptr, n_frames, height, width, lines, n_lines, idxs,
+                                     idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                     grad_lines, workspace, workspace_bytes, checkpoint_capacity,
+                                     stream, target);
+}
+
+int cbc_squared_loss_backward_f64(const double *image, const double *target, int64_t n_frames,
+                                  int64_t height, int64_t width, const double *lines,
+                                  int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                  double max_val, int32_t kernel, int32_t overlap,
+                                  const double *out0, int32_t *winner, double *grad_lines,
+                                  void *workspace, size_t workspace_bytes,
+                                  int64_t checkpoint_capacity, void *stream)
+{
+    if (!image || !target) return cbc::fail(CBC_ERR_INVALID, "null image or target");
+    return cbc::backward_impl<double>(nullptr, n_frames, height, width, lines, n_lines, idxs,
+                                      idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                      grad_lines, workspace, workspace_bytes,
+                                      checkpoint_capacity, stream, target);
 }
 
 }  // extern "C"

@@ -797,7 +797,9 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
  *            popcount give the positions);
  *   pixels:  whenever a ring holds 32 pixels, every lane takes one, evaluates the
  *            error E with the reference's rounding and, for E <= 1, calls
- *                act.pixel(slots, slot, x, y, E, te, ne).
+ *                act.pixel(slots, slot, x, y, E, te, ne, pre)
+ *            where pre = act.prefetch(slots, slot, x, y) was issued before the
+ *            error arithmetic (the action's global loads for the pixel).
  * A span walk ends at its first step with |ne| >= threshold (the reference's loop
  * condition) or when it leaves the frame.  The walks stay sequential per lane, as in
  * the reference, while the expensive per-pixel work runs on full warps.
@@ -916,6 +918,8 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 const unsigned q = (head + lane) & (kRing - 1);
                 const int slot = R.slot[q];
                 const RingPixel<T> v = R.px[q];
+                /* the action's own loads first: they complete under the error arithmetic */
+                const typename Act::Pre pre = act.prefetch(S, slot, v.x, v.y);
                 const EvalSlot<T> ev = S.ev[slot];
                 SlotParams<T> p;
                 p.len = ev.len;
@@ -926,7 +930,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 if (cap) p.len2 = S.len2[slot];
                 const T nf = A::nterm(v.ne, p);
                 const T E = cap ? A::error(v.te, nf, p) : A::error_inside(nf, p);
-                if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne);
+                if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne, pre);
             }
             head += n;
             __syncwarp();

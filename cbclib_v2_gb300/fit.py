@@ -14,9 +14,10 @@ from typing import List, Optional
 
 import torch
 
-from .autograd import draw_lines_fn
+from . import ndimage
+from .autograd import draw_lines_fn, squared_loss_backward
 
-__all__ = ['FitResult', 'fit_lines']
+__all__ = ['FitResult', 'fit_lines', 'squared_loss_step']
 
 
 @dataclass
@@ -37,23 +38,45 @@ def _loss(params, idxs, target, max_val, kernel, overlap):
     return ((img - target) ** 2).sum()
 
 
+def squared_loss_step(image: torch.Tensor, target: torch.Tensor, lines: torch.Tensor,
+                      idxs: Optional[torch.Tensor], max_val: float, kernel: str, overlap: str,
+                      winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Render ``lines`` into ``image`` (overwritten, frames start at zero) and return
+    the (N, 5) gradient of sum((image - target)^2): one forward kernel sequence and the
+    fused loss adjoint, with no full-frame gradient in memory."""
+    image.zero_()
+    ndimage.draw_lines(image, lines, idxs, max_val, kernel, overlap)
+    return squared_loss_backward(image, target, lines, idxs, max_val, kernel, overlap,
+                                 winner=winner)
+
+
 def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.Tensor] = None,
               *, max_val: float = 1.0, kernel: str = 'biweight', overlap: str = 'sum',
-              steps: int = 100, lr: float = 0.05, min_width: float = 0.5) -> FitResult:
+              steps: int = 100, lr: float = 0.05, min_width: float = 0.5,
+              fused: bool = True) -> FitResult:
     """Refine ``lines0`` (N, 5) so that draw_lines(lines) matches ``target`` (frames on
-    the GPU), with ``steps`` Adam steps of learning rate ``lr``."""
+    the GPU), with ``steps`` Adam steps of learning rate ``lr``.  ``fused`` takes the
+    gradient from the fused squared-loss adjoint (squared_loss_step); otherwise it goes
+    through torch autograd (draw_lines_fn and a torch loss), with the same result."""
     if not target.is_cuda:
         raise ValueError("target must be a CUDA tensor")
     params = lines0.detach().to(target.device, target.dtype).clone().requires_grad_(True)
     opt = torch.optim.Adam([params], lr=lr)
     with torch.no_grad():
         first = float(_loss(params, idxs, target, max_val, kernel, overlap))
+    image = torch.empty_like(target) if fused else None
+    winner = (torch.empty(target.shape, dtype=torch.int32, device=target.device)
+              if fused and overlap == 'max' else None)
     torch.cuda.synchronize(target.device)
     t0 = time.perf_counter()
     for _ in range(steps):
-        loss = _loss(params, idxs, target, max_val, kernel, overlap)
-        opt.zero_grad(set_to_none=True)
-        loss.backward()
+        if fused:
+            params.grad = squared_loss_step(image, target, params.detach(), idxs, max_val,
+                                            kernel, overlap, winner)
+        else:
+            loss = _loss(params, idxs, target, max_val, kernel, overlap)
+            opt.zero_grad(set_to_none=True)
+            loss.backward()
         opt.step()
         with torch.no_grad():
             params[:, 4].clamp_(min=min_width)

@@ -197,6 +197,29 @@ CBC_API int cbc_draw_lines_backward_f64(const double *grad_out, int64_t n_frames
                                         size_t workspace_bytes, int64_t checkpoint_capacity,
                                         void *stream);
 
+/* Gradient of the squared loss L = sum((image - target)^2) with respect to the line
+ * parameters, where image = out0 + draw_lines(lines) is the forward result (out0 NULL:
+ * zeros).  Same as cbc_draw_lines_backward_* with grad_out = 2 (image - target), which
+ * is formed per drawn pixel instead of being stored: the fused render -> loss ->
+ * adjoint step of a streak fit.  No counterpart in the reference (new). */
+CBC_API int cbc_squared_loss_backward_f32(const float *image, const float *target,
+                                          int64_t n_frames, int64_t height, int64_t width,
+                                          const float *lines, int64_t n_lines, const void *idxs,
+                                          int32_t idx_bytes, float max_val, int32_t kernel,
+                                          int32_t overlap, const float *out0, int32_t *winner,
+                                          float *grad_lines, void *workspace,
+                                          size_t workspace_bytes, int64_t checkpoint_capacity,
+                                          void *stream);
+
+CBC_API int cbc_squared_loss_backward_f64(const double *image, const double *target,
+                                          int64_t n_frames, int64_t height, int64_t width,
+                                          const double *lines, int64_t n_lines,
+                                          const void *idxs, int32_t idx_bytes, double max_val,
+                                          int32_t kernel, int32_t overlap, const double *out0,
+                                          int32_t *winner, double *grad_lines, void *workspace,
+                                          size_t workspace_bytes, int64_t checkpoint_capacity,
+                                          void *stream);
+
 /* accumulate_lines for 2-D lines.  Replaces bresenham.accumulate_lines
  * (_src/src/bresenham.cpp:301-327, accumulate_lines_nd_impl :151-259) and
  * cuda_draw_lines.accumulate_lines (_src/src/cuda_draw_lines.cu:1049-1057, 1077-1095).

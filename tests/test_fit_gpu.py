@@ -29,3 +29,39 @@ def test_fit_recovers_perturbed_lines(cuda, overlap):
 def test_fit_rejects_host_target():
     with pytest.raises(ValueError):
         fit.fit_lines(torch.zeros(1, 8, 8), torch.zeros(1, 5))
+
+
+@pytest.mark.parametrize("overlap", ['max', 'sum'])
+def test_fused_squared_loss_gradient_matches_autograd(cuda, overlap):
+    """the fused loss adjoint forms 2 (I - T) per drawn pixel: the same gradient as
+    torch autograd through draw_lines_fn and a torch loss"""
+    from cbclib_v2_gb300 import autograd
+    ls = workloads.fit_loop_stack(seed=9, F=2, H=200, W=180, per_frame=80)
+    lines = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+    target = torch.rand(ls.shape, device='cuda') * 50
+    p = lines.clone().requires_grad_(True)
+    img = autograd.draw_lines_fn(p, idxs, shape=ls.shape, max_val=ls.max_val, kernel=ls.kernel,
+                                 overlap=overlap)
+    ((img - target) ** 2).sum().backward()
+    image = torch.empty_like(target)
+    g = fit.squared_loss_step(image, target, lines, idxs, ls.max_val, ls.kernel, overlap)
+    if overlap == 'max':
+        assert torch.equal(image, img.detach())
+    else:                   # sum overlap: addition order differs between two renders
+        torch.testing.assert_close(image, img.detach(), rtol=1e-5, atol=1e-4)
+    torch.testing.assert_close(g, p.grad, rtol=1e-5, atol=1e-3)
+
+
+def test_fit_fused_and_autograd_paths_agree(cuda):
+    ls = workloads.fit_loop_stack(seed=10, F=1, H=160, W=160, per_frame=40)
+    truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+    target = torch.zeros(ls.shape, device='cuda')
+    draw_lines(target, truth, idxs, ls.max_val, ls.kernel, 'sum')
+    start = torch.from_numpy(workloads.perturbed(ls.lines, 11, 1.0, 0.3).astype(np.float32)).cuda()
+    a = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel, overlap='sum',
+                      steps=20, fused=True)
+    b = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel, overlap='sum',
+                      steps=20, fused=False)
+    torch.testing.assert_close(a.lines, b.lines, rtol=1e-4, atol=1e-3)
