@@ -96,21 +96,26 @@ struct BackwardAct {
             if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
         }
     }
+    /* max overlap: the winner first, the gradient only for the winning line; sum: the
+     * gradient of every pixel */
     struct Pre {
         int win;
         T g;
     };
+    __device__ __forceinline__ T grad_at(long long at) const {
+        return grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
+    }
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
         const long long at = S.fbase[slot] + (long long)py * W + px;
         Pre p;
         p.win = OV == CBC_MAX ? winner[at] : 0;
-        p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
+        p.g = OV == CBC_MAX ? T(0) : grad_at(at);
         return p;
     }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
                                           T, const Pre &p) {
         if (OV == CBC_MAX && p.win != S.line[slot]) return;
-        const T g = p.g;
+        const T g = OV == CBC_MAX ? grad_at(S.fbase[slot] + (long long)py * W + px) : p.g;
         if (g == T(0)) return;
         const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
         const T w = S.w[slot];
