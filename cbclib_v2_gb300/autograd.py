@@ -25,7 +25,7 @@ _workspaces = {}
 def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dtype, dev,
               grad_out: Optional[torch.Tensor] = None, image: Optional[torch.Tensor] = None,
               out0: Optional[torch.Tensor] = None, winner: Optional[torch.Tensor] = None,
-              target: Optional[torch.Tensor] = None) -> torch.Tensor:
+              target: Optional[torch.Tensor] = None, winner_known: bool = False) -> torch.Tensor:
     """One adjoint call: with grad_out, cbc_draw_lines_backward_*; with target instead,
     cbc_squared_loss_backward_* (grad_out = 2 (image - target) formed per pixel)."""
     k, ov = ndimage._check_names(kernel, overlap)
@@ -49,29 +49,20 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     lib = _native.lib()
     elem = 4 if dtype == torch.float32 else 8
     sfx = 'f32' if elem == 4 else 'f64'
-    if target is None:
-        g = grad_out.contiguous()
-        fn = getattr(lib, 'cbc_draw_lines_backward_' + sfx)
+    g = None if grad_out is None else grad_out.contiguous()
+    tg = None if target is None else target.to(dtype).contiguous()
+    if g is None and (tg is None or img is None):
+        raise ValueError("give grad_out, or the forward image and a target")
+    fn = getattr(lib, 'cbc_draw_lines_backward_ex_' + sfx)
 
-        def call(buf, ck_capacity, stream):
-            return fn(g.data_ptr(), F, H, W, ln.data_ptr(), n,
-                      None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
-                      max_val, k, ov, None if img is None else img.data_ptr(),
-                      None if o0 is None else o0.data_ptr(),
-                      None if winner is None else winner.data_ptr(), grad.data_ptr(),
-                      buf.data_ptr(), buf.numel(), ck_capacity, stream)
-    else:
-        tg = target.to(dtype).contiguous()
-        if img is None:
-            raise ValueError("the squared loss needs the forward image")
-        fn = getattr(lib, 'cbc_squared_loss_backward_' + sfx)
-
-        def call(buf, ck_capacity, stream):
-            return fn(img.data_ptr(), tg.data_ptr(), F, H, W, ln.data_ptr(), n,
-                      None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
-                      max_val, k, ov, None if o0 is None else o0.data_ptr(),
-                      None if winner is None else winner.data_ptr(), grad.data_ptr(),
-                      buf.data_ptr(), buf.numel(), ck_capacity, stream)
+    def call(buf, ck_capacity, stream):
+        return fn(None if g is None else g.data_ptr(), None if tg is None else tg.data_ptr(),
+                  F, H, W, ln.data_ptr(), n,
+                  None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                  max_val, k, ov, None if img is None else img.data_ptr(),
+                  None if o0 is None else o0.data_ptr(),
+                  None if winner is None else winner.data_ptr(), int(bool(winner_known)),
+                  grad.data_ptr(), buf.data_ptr(), buf.numel(), ck_capacity, stream)
     with ndimage._on_current_device(dev):
         stream = ndimage._current_stream(dev)
         key = ('adjoint', dev.index, stream, threading.get_ident())
@@ -113,13 +104,17 @@ def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[t
 def squared_loss_backward(image: torch.Tensor, target: torch.Tensor, lines: torch.Tensor,
                           idxs: Optional[torch.Tensor], max_val: float, kernel: str,
                           overlap: str, out0: Optional[torch.Tensor] = None,
-                          winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+                          winner: Optional[torch.Tensor] = None,
+                          winner_known: bool = False) -> torch.Tensor:
     """(N, 5) gradient of sum((image - target)^2) with respect to ``lines``, where
     ``image = out0 + draw_lines(lines, ...)`` is the forward result (``out0`` None:
     zeros).  The adjoint kernels form 2 (image - target) at each drawn pixel, so no
-    full-frame gradient is stored (the fused loss step of a streak fit)."""
+    full-frame gradient is stored (the fused loss step of a streak fit).  With
+    ``winner_known``, ``winner`` holds the forward's winners (draw_lines_max_winner) and
+    the winner pass is skipped."""
     return _backward(lines, idxs, max_val, kernel, overlap, image.shape, image.dtype,
-                     image.device, image=image, out0=out0, winner=winner, target=target)
+                     image.device, image=image, out0=out0, winner=winner, target=target,
+                     winner_known=winner_known)
 
 
 class DrawLinesFunction(torch.autograd.Function):
@@ -127,10 +122,19 @@ class DrawLinesFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, lines, out0, idxs, max_val, kernel, overlap, zero_base=False):
-        image = out0.detach().clone(memory_format=torch.contiguous_format)
         k, ov = ndimage._check_names(kernel, overlap)
-        ndimage._draw_lines_cuda(image, lines.detach(), idxs, max_val, k, ov)
         ctx.meta = (max_val, kernel, overlap)
+        ctx.winner = None
+        if overlap == 'max' and zero_base and out0.dtype == torch.float32 and \
+                lines.shape[-1] == 5:
+            # the forward records each pixel's winner: the adjoint skips its winner pass
+            image = torch.empty_like(out0, memory_format=torch.contiguous_format)
+            ctx.winner = ndimage.draw_lines_max_winner(image, lines.detach(), idxs, max_val,
+                                                       kernel)
+            ctx.save_for_backward(lines.detach(), idxs, image, None)
+            return image
+        image = out0.detach().clone(memory_format=torch.contiguous_format)
+        ndimage._draw_lines_cuda(image, lines.detach(), idxs, max_val, k, ov)
         if overlap == 'max':
             # frames that started at zero need no out0 in the winner pass
             ctx.save_for_backward(lines.detach(), idxs, image,
@@ -148,13 +152,16 @@ class DrawLinesFunction(torch.autograd.Function):
         g = grad_image.contiguous()
         if overlap == 'max':
             image, out0 = saved[2], saved[3]
-            winner = torch.empty(g.shape, dtype=torch.int32, device=g.device)
-            if ctx.needs_input_grad[0]:
-                grad_lines = lines_backward(g, lines, idxs, max_val, kernel, overlap, image,
-                                            out0, winner)
+            known = ctx.winner is not None
+            winner = ctx.winner if known else torch.empty(g.shape, dtype=torch.int32,
+                                                          device=g.device)
+            if ctx.needs_input_grad[0] or not known:
+                gl = _backward(lines, idxs, max_val, kernel, overlap, g.shape, g.dtype, g.device,
+                               grad_out=g, image=image, out0=out0, winner=winner,
+                               winner_known=known)
+                if ctx.needs_input_grad[0]:
+                    grad_lines = gl
             if ctx.needs_input_grad[1]:
-                if not ctx.needs_input_grad[0]:
-                    lines_backward(g, lines, idxs, max_val, kernel, overlap, image, out0, winner)
                 grad_out0 = torch.where(winner == _native.NO_WINNER, g, torch.zeros_like(g))
         else:
             if ctx.needs_input_grad[0]:

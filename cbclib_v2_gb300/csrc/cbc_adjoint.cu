@@ -206,16 +206,18 @@ AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes,
 }
 
 template <typename T, int K>
-cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, cudaStream_t s)
+cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, bool winner_known, cudaStream_t s)
 {
     if (overlap == CBC_MAX) {
-        const unsigned grid = resident_grid(winner_kernel<T, K>, kSegWarps * 32);
-        winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
-        note_launches(1);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
-        if (e != cudaSuccess) return e;
+        if (!winner_known) {
+            const unsigned grid = resident_grid(winner_kernel<T, K>, kSegWarps * 32);
+            winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
+            note_launches(1);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
+            if (e != cudaSuccess) return e;
+        }
         backward_kernel<T, K, CBC_MAX><<<resident_grid(backward_kernel<T, K, CBC_MAX>,
                                                        kSegWarps * 32),
                                          kSegWarps * 32, 0, s>>>(aa);
@@ -233,7 +235,8 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
                   const T *lines, long long n_lines, const void *idxs, int idx_bytes,
                   T max_val, int kernel, int overlap, const T *image, const T *out0,
                   int *winner, T *grad_lines, void *workspace, size_t ws_bytes,
-                  long long ck_capacity, void *stream, const T *target = nullptr)
+                  long long ck_capacity, void *stream, const T *target = nullptr,
+                  bool winner_known = false)
 {
     clear_error();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
@@ -292,7 +295,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (pixels) {
-        if (overlap == CBC_MAX) {
+        if (overlap == CBC_MAX && !winner_known) {
             e = cudaMemsetAsync(winner, 0x7f, sizeof(int) * (size_t)(n_frames * H * W), s);
             if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         }
@@ -311,11 +314,11 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.gacc = gacc;
         aa.max_val = max_val;
         switch (kernel) {
-        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, s); break;
-        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, s); break;
-        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, s); break;
-        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, s); break;
-        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, s); break;
+        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, winner_known, s); break;
+        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, winner_known, s); break;
+        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, winner_known, s); break;
+        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, winner_known, s); break;
+        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, winner_known, s); break;
         }
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     }
@@ -396,6 +399,39 @@ int cbc_squared_loss_backward_f64(const double *image, const double *target, int
                                       idx_bytes, max_val, kernel, overlap, image, out0, winner,
                                       grad_lines, workspace, workspace_bytes,
                                       checkpoint_capacity, stream, target);
+}
+
+int cbc_draw_lines_backward_ex_f32(const float *grad_out, const float *target, int64_t n_frames,
+                                   int64_t height, int64_t width, const float *lines,
+                                   int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                   float max_val, int32_t kernel, int32_t overlap,
+                                   const float *image, const float *out0, int32_t *winner,
+                                   int32_t winner_known, float *grad_lines, void *workspace,
+                                   size_t workspace_bytes, int64_t checkpoint_capacity,
+                                   void *stream)
+{
+    if (!grad_out && !(image && target)) return cbc::fail(CBC_ERR_INVALID, "null grad_out");
+    return cbc::backward_impl<float>(grad_out, n_frames, height, width, lines, n_lines, idxs,
+                                     idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                     grad_lines, workspace, workspace_bytes, checkpoint_capacity,
+                                     stream, grad_out ? nullptr : target, winner_known != 0);
+}
+
+int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double *target, int64_t n_frames,
+                                   int64_t height, int64_t width, const double *lines,
+                                   int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                   double max_val, int32_t kernel, int32_t overlap,
+                                   const double *image, const double *out0, int32_t *winner,
+                                   int32_t winner_known, double *grad_lines, void *workspace,
+                                   size_t workspace_bytes, int64_t checkpoint_capacity,
+                                   void *stream)
+{
+    if (!grad_out && !(image && target)) return cbc::fail(CBC_ERR_INVALID, "null grad_out");
+    return cbc::backward_impl<double>(grad_out, n_frames, height, width, lines, n_lines, idxs,
+                                      idx_bytes, max_val, kernel, overlap, image, out0, winner,
+                                      grad_lines, workspace, workspace_bytes,
+                                      checkpoint_capacity, stream, grad_out ? nullptr : target,
+                                      winner_known != 0);
 }
 
 }  // extern "C"

@@ -327,6 +327,69 @@ struct ForwardAct {
     }
 };
 
+/* max overlap into frames that start at zero, keeping each pixel's winner: the value's
+ * bits (positive floats order as integers) over the complement of the line index, so
+ * one 64-bit atomicMax keeps the largest value and, among equal values, the smallest
+ * line, which is the line sequential std::max keeps (bresenham.cpp:71) */
+template <int K>
+struct PackedMaxAct {
+    static constexpr bool kNeedsGeometry = false;
+    unsigned long long *packed;
+    float max_val;
+    int W;
+    const float *gtab;
+    struct Pre {};
+    __device__ __forceinline__ void item_begin(int) {}
+    __device__ __forceinline__ void item_end(int, const SlotTable<float> &) {}
+    __device__ __forceinline__ Pre prefetch(const SlotTable<float> &, int, int, int) const {
+        return {};
+    }
+    __device__ __forceinline__ void pixel(const SlotTable<float> &S, int slot, int px, int py,
+                                          float E, float, float, Pre) {
+        using A = Ar<float>;
+        const float v = A::mul(max_val, A::template profile_tab<K>(A::sqrt(E), gtab));
+        if (!(v > 0.0f)) return;      /* std::max(0, v) keeps the zero */
+        const unsigned long long key =
+            ((unsigned long long)__float_as_uint(v) << 32) |
+            (unsigned long long)(0xffffffffu - (unsigned)S.line[slot]);
+        atomicMax(packed + S.fbase[slot] + (long long)py * W + px, key);
+    }
+};
+
+struct PackedArgs {
+    DriveArgs<float> d;
+    unsigned long long *packed;
+    float max_val;
+};
+
+template <int K>
+__global__ void __launch_bounds__(kSegWarps * 32, kSegMinBlocks)
+packed_max_kernel(PackedArgs a)
+{
+    PackedMaxAct<K> act;
+    act.packed = a.packed;
+    act.max_val = a.max_val;
+    act.W = a.d.W;
+    act.gtab = stage_gauss_table<float, K>();
+    drive_segments(a.d, act);
+}
+
+/* packed -> frames and winners; packed is left zero for the next call */
+static __global__ void __launch_bounds__(kThreads)
+unpack_max_kernel(unsigned long long *__restrict__ packed, float *__restrict__ out,
+                  int *__restrict__ winner, long long n, const DevStatus *st)
+{
+    if (st->flags & kFatal) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long k = packed[i];
+        const unsigned hi = (unsigned)(k >> 32);
+        out[i] = __uint_as_float(hi);
+        winner[i] = hi ? (int)(0xffffffffu - (unsigned)k) : 0x7f7f7f7f;
+        if (k) packed[i] = 0ull;
+    }
+}
+
 template <typename T>
 struct SegArgs {
     DriveArgs<T> d;
@@ -557,7 +620,8 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
                     long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel,
                     int overlap, void *workspace, size_t ws_bytes, long long capacity,
                     long long ck_capacity, const cbc_tuning *tuning, void *stream,
-                    const int64_t *csr = nullptr)
+                    const int64_t *csr = nullptr, unsigned long long *packed = nullptr,
+                    int *winner = nullptr)
 {
     g_error.clear();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
@@ -640,7 +704,44 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
         timer.mark(1);
         timer.mark(2);
         timer.mark(3);
-        if (n_frames * H * W > 0) {
+        if (n_frames * H * W > 0 && packed) {
+            if constexpr (sizeof(T) == sizeof(float)) {
+                PackedArgs pa;
+                pa.packed = packed;
+                pa.max_val = max_val;
+                pa.d.recs = reinterpret_cast<const LineRec<float> *>(recs);
+                pa.d.cks = reinterpret_cast<const Checkpoint<float> *>(cks);
+                pa.d.H = (int)H;
+                pa.d.W = (int)W;
+                pa.d.st = st;
+                pa.d.work = &st->work;
+                const unsigned threads = kSegWarps * 32;
+#define CBC_PACKED_CASE(KK)                                                                   \
+                case KK:                                                                    \
+                    packed_max_kernel<KK><<<resident_grid(packed_max_kernel<KK>, threads),   \
+                                            threads, 0, s>>>(pa);                           \
+                    break;
+                switch (kernel) {
+                CBC_PACKED_CASE(CBC_BIWEIGHT)
+                CBC_PACKED_CASE(CBC_GAUSSIAN)
+                CBC_PACKED_CASE(CBC_PARABOLIC)
+                CBC_PACKED_CASE(CBC_RECTANGULAR)
+                default: CBC_PACKED_CASE(CBC_TRIANGULAR)
+                }
+#undef CBC_PACKED_CASE
+                const long long n = n_frames * H * W;
+                int dev = 0, sms = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                long long blocks = (n + kThreads - 1) / kThreads;
+                if (blocks > (long long)(sms > 0 ? sms : 132) * 16) blocks = (long long)(sms > 0 ? sms : 132) * 16;
+                unpack_max_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(
+                    packed, reinterpret_cast<float *>(out), winner, n, st);
+                note_launches(2);
+                e = cudaGetLastError();
+                if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+            }
+        } else if (n_frames * H * W > 0) {
             SegArgs<T> sg;
             sg.out = out;
             sg.max_val = max_val;
@@ -772,6 +873,24 @@ int cbc_draw_lines_csr_f64(double *out, int64_t n_frames, int64_t height, int64_
                                         max_val, kernel, overlap, workspace, workspace_bytes,
                                         pair_capacity, checkpoint_capacity, tuning, stream,
                                         frame_offsets);
+}
+
+int cbc_draw_lines_max_winner_f32(float *out, int32_t *winner, uint64_t *packed,
+                                  int64_t n_frames, int64_t height, int64_t width,
+                                  const float *lines, int64_t n_lines, const void *idxs,
+                                  int32_t idx_bytes, float max_val, int32_t kernel,
+                                  void *workspace, size_t workspace_bytes, int64_t pair_capacity,
+                                  int64_t checkpoint_capacity, void *stream)
+{
+    if (n_lines > 0 && n_frames * height * width > 0 && (!out || !winner || !packed))
+        return cbc::fail(CBC_ERR_INVALID, "null out, winner or packed");
+    cbc_tuning t{};
+    t.strategy = CBC_STRATEGY_LINES;
+    return cbc::draw_lines_impl<float>(out, n_frames, height, width, lines, n_lines, idxs,
+                                       idx_bytes, max_val, kernel, CBC_MAX, workspace,
+                                       workspace_bytes, pair_capacity, checkpoint_capacity, &t,
+                                       stream, nullptr,
+                                       reinterpret_cast<unsigned long long *>(packed), winner);
 }
 
 int cbc_read_status(const void *workspace, cbc_status *status, void *stream)

@@ -44,6 +44,11 @@ def squared_loss_step(image: torch.Tensor, target: torch.Tensor, lines: torch.Te
     """Render ``lines`` into ``image`` (overwritten, frames start at zero) and return
     the (N, 5) gradient of sum((image - target)^2): one forward kernel sequence and the
     fused loss adjoint, with no full-frame gradient in memory."""
+    if overlap == 'max' and image.dtype == torch.float32:
+        # the forward records the winners: no winner pass in the adjoint
+        winner = ndimage.draw_lines_max_winner(image, lines, idxs, max_val, kernel, winner)
+        return squared_loss_backward(image, target, lines, idxs, max_val, kernel, overlap,
+                                     winner=winner, winner_known=True)
     image.zero_()
     ndimage.draw_lines(image, lines, idxs, max_val, kernel, overlap)
     return squared_loss_backward(image, target, lines, idxs, max_val, kernel, overlap,

@@ -328,6 +328,60 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
     return out
 
 
+_packed: dict = {}
+
+
+def _packed_scratch(dev: torch.device, n: int) -> torch.Tensor:
+    """this thread's zeroed uint64 scratch of at least n values on the current stream of
+    `dev` (the library leaves it zero after every call)"""
+    key = (dev.index, _current_stream(dev), threading.get_ident())
+    buf = _packed.get(key)
+    if buf is None or buf.numel() < n:
+        buf = _packed[key] = torch.zeros(n, dtype=torch.int64, device=dev)
+    return buf
+
+
+def draw_lines_max_winner(out: torch.Tensor, lines, idxs=None, max_val: float = 1.0,
+                          kernel: str = 'rectangular',
+                          winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Max-overlap draw_lines into float32 CUDA frames that start at zero (``out`` is
+    overwritten) and the winner of every pixel: the line whose value the pixel holds
+    (the smallest index among equal values, as sequential std::max keeps), or
+    0x7f7f7f7f where no line raised the pixel above zero.  Returns ``winner`` (int32,
+    the frames' shape; allocated when not given)."""
+    k, _ = _check_names(kernel, 'max')
+    if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float32):
+        raise TypeError("out must be a float32 CUDA tensor")
+    F, H, W = _frames_of(out)
+    dev = out.device
+    ln = _as_device_lines(lines, dev, out.dtype)
+    if ln.shape[1] != 5:
+        raise ValueError("draw_lines_max_winner takes 2-D lines (N, 5)")
+    n_lines = ln.shape[0]
+    ix = _as_device_idxs(idxs, n_lines, dev)
+    if ix is None and n_lines and F != 1 and F != n_lines:
+        raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
+    if winner is None:
+        winner = torch.empty(out.shape, dtype=torch.int32, device=dev)
+    work = out if out.is_contiguous() else torch.empty(out.shape, dtype=out.dtype, device=dev)
+    packed = _packed_scratch(dev, F * H * W)
+    lib = _native.lib()
+    t = _native.Tuning()
+    t.strategy = _native.STRATEGY_LINES
+
+    def call(buf, capacity, ck_capacity, tref, stream):
+        return lib.cbc_draw_lines_max_winner_f32(
+            work.data_ptr(), winner.data_ptr(), packed.data_ptr(), F, H, W, ln.data_ptr(),
+            n_lines, None if ix is None else ix.data_ptr(),
+            0 if ix is None else ix.element_size(), max_val, k, buf.data_ptr(), buf.numel(),
+            capacity, ck_capacity, stream)
+
+    _run_with_workspace(call, dev, F, H, W, n_lines, 4, t)
+    if work is not out:
+        out.copy_(work)
+    return winner
+
+
 def draw_lines_csr(out: torch.Tensor, lines, frame_offsets, max_val: float = 1.0,
                    kernel: str = 'rectangular', overlap: str = 'sum',
                    tuning: Optional[_native.Tuning] = None) -> torch.Tensor:

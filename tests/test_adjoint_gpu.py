@@ -174,3 +174,31 @@ def test_forward_matches_in_place_draw_lines(cuda):
             assert torch.equal(a, b)
         else:                      # sum: the order of float additions may differ
             assert torch.allclose(a, b, rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'triangular', 'rectangular'])
+def test_max_winner_forward_matches_draw_and_winner_pass(cuda, kernel):
+    """draw_lines_max_winner: the same frames as draw_lines(max) from zero, and the same
+    winners as the adjoint's own winner pass"""
+    import numpy as np
+    import torch
+    from cbclib_v2_gb300 import autograd, ndimage
+    rng = np.random.default_rng(21)
+    F, H, W, n = 2, 90, 110, 150
+    p0 = rng.random((n, 2)) * [W, H]
+    v = rng.normal(size=(n, 2))
+    p1 = p0 + v / np.linalg.norm(v, axis=1, keepdims=True) * rng.uniform(3, 40, n)[:, None]
+    lines = torch.from_numpy(np.concatenate([p0, p1, rng.uniform(1, 5, (n, 1))], 1)
+                             .astype(np.float32)).cuda()
+    idxs = torch.from_numpy(rng.integers(0, F, n).astype(np.int32)).cuda()
+    img = torch.full((F, H, W), 7.0, device='cuda')         # overwritten
+    win = ndimage.draw_lines_max_winner(img, lines, idxs, 2.0, kernel)
+    ref = torch.zeros((F, H, W), device='cuda')
+    ndimage.draw_lines(ref, lines, idxs, 2.0, kernel, 'max')
+    assert torch.equal(img, ref)
+    w2 = torch.empty((F, H, W), dtype=torch.int32, device='cuda')
+    autograd.lines_backward(torch.ones_like(ref), lines, idxs, 2.0, kernel, 'max', ref, None, w2)
+    assert torch.equal(win, w2)
+    again = torch.empty_like(img)                           # the scratch was left zero
+    assert torch.equal(ndimage.draw_lines_max_winner(again, lines, idxs, 2.0, kernel), win)
+    assert torch.equal(again, ref)
