@@ -32,6 +32,7 @@ namespace cbc {
 template <typename T, int K>
 struct WinnerAct {
     static constexpr bool kNeedsGeometry = false;
+    static constexpr bool kNeedsError = true;
     const T *image;
     const T *out0;       /* NULL: zeros */
     int *winner;
@@ -75,6 +76,9 @@ __device__ __forceinline__ T kappa_of(T d, T w, T max_val)
 template <typename T, int K, int OV>
 struct BackwardAct {
     static constexpr bool kNeedsGeometry = true;
+    /* max overlap: a pixel whose winner is this line was drawn by it, so the error is
+     * not needed; sum overlap: every drawn pixel (error <= 1) */
+    static constexpr bool kNeedsError = OV != CBC_MAX;
     const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
     const T *image;
     const T *target;

@@ -804,7 +804,8 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
  * condition) or when it leaves the frame.  The walks stay sequential per lane, as in
  * the reference, while the expensive per-pixel work runs on full warps.
  * act.item_begin(lane) / act.item_end(lane, slots) bracket each warp item; an action
- * that reads the line geometry from the slot table sets kNeedsGeometry.  The forward,
+ * that reads the line geometry from the slot table sets kNeedsGeometry, one that needs
+ * no error (and is handed every visited pixel) clears kNeedsError.  The forward,
  * the max-overlap winner pass and the adjoint are such actions. */
 
 constexpr int kSegWarps = 4;
@@ -920,17 +921,23 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 const RingPixel<T> v = R.px[q];
                 /* the action's own loads first: they complete under the error arithmetic */
                 const typename Act::Pre pre = act.prefetch(S, slot, v.x, v.y);
-                const EvalSlot<T> ev = S.ev[slot];
-                SlotParams<T> p;
-                p.len = ev.len;
-                p.rlen = ev.rlen;
-                p.ww = ev.ww;
-                p.rww = ev.rww;
-                p.fast = S.fast[slot];
-                if (cap) p.len2 = S.len2[slot];
-                const T nf = A::nterm(v.ne, p);
-                const T E = cap ? A::error(v.te, nf, p) : A::error_inside(nf, p);
-                if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne, pre);
+                if constexpr (Act::kNeedsError) {
+                    const EvalSlot<T> ev = S.ev[slot];
+                    SlotParams<T> p;
+                    p.len = ev.len;
+                    p.rlen = ev.rlen;
+                    p.ww = ev.ww;
+                    p.rww = ev.rww;
+                    p.fast = S.fast[slot];
+                    if (cap) p.len2 = S.len2[slot];
+                    const T nf = A::nterm(v.ne, p);
+                    const T E = cap ? A::error(v.te, nf, p) : A::error_inside(nf, p);
+                    if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne, pre);
+                } else {
+                    /* the action decides from its own data which visited pixels count
+                     * (the max-overlap adjoint: the pixel's winner) */
+                    act.pixel(S, slot, v.x, v.y, T(0), v.te, v.ne, pre);
+                }
             }
             head += n;
             __syncwarp();

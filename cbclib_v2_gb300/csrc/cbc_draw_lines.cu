@@ -310,6 +310,7 @@ render_kernel(RenderArgs<T> a)
 template <typename T, int K, int OV>
 struct ForwardAct {
     static constexpr bool kNeedsGeometry = false;
+    static constexpr bool kNeedsError = true;
     T *out;
     T max_val;
     int W;
@@ -334,6 +335,7 @@ struct ForwardAct {
 template <int K>
 struct PackedMaxAct {
     static constexpr bool kNeedsGeometry = false;
+    static constexpr bool kNeedsError = true;
     unsigned long long *packed;
     float max_val;
     int W;
