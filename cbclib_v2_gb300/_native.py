@@ -124,7 +124,7 @@ def _declare(lib):
     for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
         f = getattr(lib, 'cbc_draw_lines_backward_ex_' + sfx)
         f.argtypes = [p, p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, p, p, i32, p, p,
-                      ctypes.c_size_t, i64, p]
+                      p, ctypes.c_size_t, i64, p]
         f.restype = ctypes.c_int
     lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
     lib.cbc_read_status.restype = ctypes.c_int

@@ -25,7 +25,8 @@ _workspaces = {}
 def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dtype, dev,
               grad_out: Optional[torch.Tensor] = None, image: Optional[torch.Tensor] = None,
               out0: Optional[torch.Tensor] = None, winner: Optional[torch.Tensor] = None,
-              target: Optional[torch.Tensor] = None, winner_known: bool = False) -> torch.Tensor:
+              target: Optional[torch.Tensor] = None, winner_known: bool = False,
+              packed: Optional[torch.Tensor] = None) -> torch.Tensor:
     """One adjoint call: with grad_out, cbc_draw_lines_backward_*; with target instead,
     cbc_squared_loss_backward_* (grad_out = 2 (image - target) formed per pixel)."""
     k, ov = ndimage._check_names(kernel, overlap)
@@ -40,7 +41,7 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     F = math.prod(int(s) for s in shape[:-2])
     img = None if image is None else image.to(dtype).contiguous()
     o0 = None if out0 is None else out0.to(dtype).contiguous()
-    if ov == _native.OVERLAPS['max']:
+    if ov == _native.OVERLAPS['max'] and packed is None:
         if img is None:
             raise ValueError("max overlap needs the forward image")
         if winner is None:
@@ -51,7 +52,7 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     sfx = 'f32' if elem == 4 else 'f64'
     g = None if grad_out is None else grad_out.contiguous()
     tg = None if target is None else target.to(dtype).contiguous()
-    if g is None and (tg is None or img is None):
+    if g is None and (tg is None or (img is None and packed is None)):
         raise ValueError("give grad_out, or the forward image and a target")
     fn = getattr(lib, 'cbc_draw_lines_backward_ex_' + sfx)
 
@@ -62,6 +63,7 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
                   max_val, k, ov, None if img is None else img.data_ptr(),
                   None if o0 is None else o0.data_ptr(),
                   None if winner is None else winner.data_ptr(), int(bool(winner_known)),
+                  None if packed is None else packed.data_ptr(),
                   grad.data_ptr(), buf.data_ptr(), buf.numel(), ck_capacity, stream)
     with ndimage._on_current_device(dev):
         stream = ndimage._current_stream(dev)

@@ -82,6 +82,7 @@ struct BackwardAct {
     const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
     const T *image;
     const T *target;
+    const unsigned long long *packed;   /* max overlap: (value bits, ~winner) per pixel */
     const int *winner;   /* max overlap */
     double *gacc;        /* (N, 5) */
     T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
@@ -112,14 +113,24 @@ struct BackwardAct {
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
         const long long at = S.fbase[slot] + (long long)py * W + px;
         Pre p;
-        p.win = OV == CBC_MAX ? winner[at] : 0;
-        p.g = OV == CBC_MAX ? T(0) : grad_at(at);
+        if (OV == CBC_MAX && packed) {
+            /* value and winner in one load, the target beside it: the squared-loss
+             * gradient of the winning line needs no second round trip */
+            const unsigned long long k = packed[at];
+            const unsigned hi = (unsigned)(k >> 32);
+            p.win = hi ? (int)(0xffffffffu - (unsigned)k) : 0x7f7f7f7f;
+            p.g = target ? T(2) * ((T)__uint_as_float(hi) - target[at]) : T(0);
+        } else {
+            p.win = OV == CBC_MAX ? winner[at] : 0;
+            p.g = OV == CBC_MAX ? T(0) : grad_at(at);
+        }
         return p;
     }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
                                           T, const Pre &p) {
         if (OV == CBC_MAX && p.win != S.line[slot]) return;
-        const T g = OV == CBC_MAX ? grad_at(S.fbase[slot] + (long long)py * W + px) : p.g;
+        const T g = (OV == CBC_MAX && !(packed && target))
+                        ? grad_at(S.fbase[slot] + (long long)py * W + px) : p.g;
         if (g == T(0)) return;
         const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
         const T w = S.w[slot];
@@ -149,6 +160,7 @@ struct AdjArgs {
     const T *image;
     const T *out0;
     const T *target;
+    const unsigned long long *packed;
     int *winner;
     double *gacc;
     T max_val;
@@ -177,6 +189,7 @@ backward_kernel(AdjArgs<T> a)
     act.grad_out = a.grad_out;
     act.image = a.image;
     act.target = a.target;
+    act.packed = a.packed;
     act.winner = a.winner;
     act.gacc = a.gacc;
     act.acc = acc_s[threadIdx.x >> 5];
@@ -240,8 +253,9 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
                   T max_val, int kernel, int overlap, const T *image, const T *out0,
                   int *winner, T *grad_lines, void *workspace, size_t ws_bytes,
                   long long ck_capacity, void *stream, const T *target = nullptr,
-                  bool winner_known = false)
+                  bool winner_known = false, const unsigned long long *packed = nullptr)
 {
+    if (packed) winner_known = true;
     clear_error();
     if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0)
         return fail(CBC_ERR_INVALID, "negative size");
@@ -260,10 +274,12 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
     const bool pixels = n_frames * H * W > 0;
     if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
-    if (n_lines > 0 && pixels && !grad_out && !(target && image))
+    if (n_lines > 0 && pixels && !grad_out && !(target && (image || packed)))
         return fail(CBC_ERR_INVALID, "null grad_out");
-    if (overlap == CBC_MAX && n_lines > 0 && pixels && (!image || !winner))
+    if (overlap == CBC_MAX && n_lines > 0 && pixels && !packed && (!image || !winner))
         return fail(CBC_ERR_INVALID, "max overlap needs the forward image and a winner buffer");
+    if (packed && (overlap != CBC_MAX || sizeof(T) != sizeof(float)))
+        return fail(CBC_ERR_INVALID, "packed winners are for float32 max overlap");
     AdjLayout L = adj_layout(n_lines, ck_capacity, sizeof(LineRec<T>), sizeof(Checkpoint<T>));
     if (!workspace || ws_bytes < L.total)
         return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
@@ -314,6 +330,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.image = image;
         aa.out0 = out0;
         aa.target = target;
+        aa.packed = packed;
         aa.winner = winner;
         aa.gacc = gacc;
         aa.max_val = max_val;
@@ -410,15 +427,17 @@ int cbc_draw_lines_backward_ex_f32(const float *grad_out, const float *target, i
                                    int64_t n_lines, const void *idxs, int32_t idx_bytes,
                                    float max_val, int32_t kernel, int32_t overlap,
                                    const float *image, const float *out0, int32_t *winner,
-                                   int32_t winner_known, float *grad_lines, void *workspace,
-                                   size_t workspace_bytes, int64_t checkpoint_capacity,
-                                   void *stream)
+                                   int32_t winner_known, const uint64_t *packed,
+                                   float *grad_lines, void *workspace, size_t workspace_bytes,
+                                   int64_t checkpoint_capacity, void *stream)
 {
-    if (!grad_out && !(image && target)) return cbc::fail(CBC_ERR_INVALID, "null grad_out");
+    if (!grad_out && !((image || packed) && target))
+        return cbc::fail(CBC_ERR_INVALID, "null grad_out");
     return cbc::backward_impl<float>(grad_out, n_frames, height, width, lines, n_lines, idxs,
                                      idx_bytes, max_val, kernel, overlap, image, out0, winner,
                                      grad_lines, workspace, workspace_bytes, checkpoint_capacity,
-                                     stream, grad_out ? nullptr : target, winner_known != 0);
+                                     stream, grad_out ? nullptr : target, winner_known != 0,
+                                     reinterpret_cast<const unsigned long long *>(packed));
 }
 
 int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double *target, int64_t n_frames,
@@ -426,10 +445,11 @@ int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double *target,
                                    int64_t n_lines, const void *idxs, int32_t idx_bytes,
                                    double max_val, int32_t kernel, int32_t overlap,
                                    const double *image, const double *out0, int32_t *winner,
-                                   int32_t winner_known, double *grad_lines, void *workspace,
-                                   size_t workspace_bytes, int64_t checkpoint_capacity,
-                                   void *stream)
+                                   int32_t winner_known, const uint64_t *packed,
+                                   double *grad_lines, void *workspace, size_t workspace_bytes,
+                                   int64_t checkpoint_capacity, void *stream)
 {
+    if (packed) return cbc::fail(CBC_ERR_INVALID, "packed winners are for float32 max overlap");
     if (!grad_out && !(image && target)) return cbc::fail(CBC_ERR_INVALID, "null grad_out");
     return cbc::backward_impl<double>(grad_out, n_frames, height, width, lines, n_lines, idxs,
                                       idx_bytes, max_val, kernel, overlap, image, out0, winner,

@@ -638,7 +638,7 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     if (!idxs && !csr && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
         return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
                                          " != " + std::to_string(n_frames) + ")");
-    if (n_lines > 0 && (!out || !lines) && n_frames * H * W > 0)
+    if (n_lines > 0 && ((!out && !packed) || !lines) && n_frames * H * W > 0)
         return fail(CBC_ERR_INVALID, "null pointer");
     if (capacity < 0 || capacity > INT_MAX) return fail(CBC_ERR_INVALID, "pair_capacity out of range");
     if (ck_capacity < 0 || ck_capacity > INT_MAX)
@@ -731,15 +731,19 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
                 default: CBC_PACKED_CASE(CBC_TRIANGULAR)
                 }
 #undef CBC_PACKED_CASE
-                const long long n = n_frames * H * W;
-                int dev = 0, sms = 0;
-                cudaGetDevice(&dev);
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                long long blocks = (n + kThreads - 1) / kThreads;
-                if (blocks > (long long)(sms > 0 ? sms : 132) * 16) blocks = (long long)(sms > 0 ? sms : 132) * 16;
-                unpack_max_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(
-                    packed, reinterpret_cast<float *>(out), winner, n, st);
-                note_launches(2);
+                note_launches(1);
+                if (out && winner) {      /* else the caller keeps the packed pairs */
+                    const long long n = n_frames * H * W;
+                    int dev = 0, sms = 0;
+                    cudaGetDevice(&dev);
+                    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                    const long long most = (long long)(sms > 0 ? sms : 132) * 16;
+                    long long blocks = (n + kThreads - 1) / kThreads;
+                    if (blocks > most) blocks = most;
+                    unpack_max_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(
+                        packed, reinterpret_cast<float *>(out), winner, n, st);
+                    note_launches(1);
+                }
                 e = cudaGetLastError();
                 if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
             }
@@ -884,8 +888,8 @@ int cbc_draw_lines_max_winner_f32(float *out, int32_t *winner, uint64_t *packed,
                                   void *workspace, size_t workspace_bytes, int64_t pair_capacity,
                                   int64_t checkpoint_capacity, void *stream)
 {
-    if (n_lines > 0 && n_frames * height * width > 0 && (!out || !winner || !packed))
-        return cbc::fail(CBC_ERR_INVALID, "null out, winner or packed");
+    if (n_lines > 0 && n_frames * height * width > 0 && (!packed || (!out != !winner)))
+        return cbc::fail(CBC_ERR_INVALID, "null packed, or only one of out and winner");
     cbc_tuning t{};
     t.strategy = CBC_STRATEGY_LINES;
     return cbc::draw_lines_impl<float>(out, n_frames, height, width, lines, n_lines, idxs,

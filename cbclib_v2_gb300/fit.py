@@ -15,7 +15,7 @@ from typing import List, Optional
 import torch
 
 from . import ndimage
-from .autograd import draw_lines_fn, squared_loss_backward
+from .autograd import _backward, draw_lines_fn, squared_loss_backward
 
 __all__ = ['FitResult', 'fit_lines', 'squared_loss_step']
 
@@ -38,12 +38,24 @@ def _loss(params, idxs, target, max_val, kernel, overlap):
     return ((img - target) ** 2).sum()
 
 
-def squared_loss_step(image: torch.Tensor, target: torch.Tensor, lines: torch.Tensor,
+def squared_loss_step(image: Optional[torch.Tensor], target: torch.Tensor, lines: torch.Tensor,
                       idxs: Optional[torch.Tensor], max_val: float, kernel: str, overlap: str,
                       winner: Optional[torch.Tensor] = None) -> torch.Tensor:
     """Render ``lines`` into ``image`` (overwritten, frames start at zero) and return
     the (N, 5) gradient of sum((image - target)^2): one forward kernel sequence and the
-    fused loss adjoint, with no full-frame gradient in memory."""
+    fused loss adjoint, with no full-frame gradient in memory.  With image None (float32
+    max overlap) the forward keeps each pixel's value and winner packed in one scratch
+    word and the adjoint reads them from there; no frames are written."""
+    if image is None:
+        if overlap != 'max' or target.dtype != torch.float32:
+            raise ValueError("image=None is for float32 max overlap")
+        packed = ndimage._max_winner(None, None, target.shape, target.device, lines, idxs,
+                                     max_val, kernel)
+        try:
+            return _backward(lines, idxs, max_val, kernel, overlap, target.shape, target.dtype,
+                             target.device, target=target, packed=packed)
+        finally:
+            packed.zero_()
     if overlap == 'max' and image.dtype == torch.float32:
         # the forward records the winners: no winner pass in the adjoint
         winner = ndimage.draw_lines_max_winner(image, lines, idxs, max_val, kernel, winner)
@@ -69,9 +81,10 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
     opt = torch.optim.Adam([params], lr=lr)
     with torch.no_grad():
         first = float(_loss(params, idxs, target, max_val, kernel, overlap))
-    image = torch.empty_like(target) if fused else None
+    packed_path = fused and overlap == 'max' and target.dtype == torch.float32
+    image = torch.empty_like(target) if fused and not packed_path else None
     winner = (torch.empty(target.shape, dtype=torch.int32, device=target.device)
-              if fused and overlap == 'max' else None)
+              if fused and overlap == 'max' and not packed_path else None)
     torch.cuda.synchronize(target.device)
     t0 = time.perf_counter()
     for _ in range(steps):

@@ -349,21 +349,33 @@ def draw_lines_max_winner(out: torch.Tensor, lines, idxs=None, max_val: float = 
     (the smallest index among equal values, as sequential std::max keeps), or
     0x7f7f7f7f where no line raised the pixel above zero.  Returns ``winner`` (int32,
     the frames' shape; allocated when not given)."""
-    k, _ = _check_names(kernel, 'max')
     if not (isinstance(out, torch.Tensor) and out.is_cuda and out.dtype == torch.float32):
         raise TypeError("out must be a float32 CUDA tensor")
-    F, H, W = _frames_of(out)
-    dev = out.device
-    ln = _as_device_lines(lines, dev, out.dtype)
+    if winner is None:
+        winner = torch.empty(out.shape, dtype=torch.int32, device=out.device)
+    work = out if out.is_contiguous() else torch.empty(out.shape, dtype=out.dtype,
+                                                       device=out.device)
+    _max_winner(work, winner, out.shape, out.device, lines, idxs, max_val, kernel)
+    if work is not out:
+        out.copy_(work)
+    return winner
+
+
+def _max_winner(out: Optional[torch.Tensor], winner: Optional[torch.Tensor], shape, dev,
+                lines, idxs, max_val: float, kernel: str) -> torch.Tensor:
+    """cbc_draw_lines_max_winner_f32 with this thread's packed scratch; with out and
+    winner None the scratch is returned holding the (value, winner) pairs and the
+    caller zeroes it after use"""
+    k, _ = _check_names(kernel, 'max')
+    H, W = int(shape[-2]), int(shape[-1])
+    F = math.prod(int(s) for s in shape[:-2])
+    ln = _as_device_lines(lines, dev, torch.float32)
     if ln.shape[1] != 5:
         raise ValueError("draw_lines_max_winner takes 2-D lines (N, 5)")
     n_lines = ln.shape[0]
     ix = _as_device_idxs(idxs, n_lines, dev)
     if ix is None and n_lines and F != 1 and F != n_lines:
         raise ValueError(f"idxs has an incompatible size ({n_lines} != {F})")
-    if winner is None:
-        winner = torch.empty(out.shape, dtype=torch.int32, device=dev)
-    work = out if out.is_contiguous() else torch.empty(out.shape, dtype=out.dtype, device=dev)
     packed = _packed_scratch(dev, F * H * W)
     lib = _native.lib()
     t = _native.Tuning()
@@ -371,15 +383,14 @@ def draw_lines_max_winner(out: torch.Tensor, lines, idxs=None, max_val: float = 
 
     def call(buf, capacity, ck_capacity, tref, stream):
         return lib.cbc_draw_lines_max_winner_f32(
-            work.data_ptr(), winner.data_ptr(), packed.data_ptr(), F, H, W, ln.data_ptr(),
+            None if out is None else out.data_ptr(), None if winner is None else winner.data_ptr(),
+            packed.data_ptr(), F, H, W, ln.data_ptr(),
             n_lines, None if ix is None else ix.data_ptr(),
             0 if ix is None else ix.element_size(), max_val, k, buf.data_ptr(), buf.numel(),
             capacity, ck_capacity, stream)
 
     _run_with_workspace(call, dev, F, H, W, n_lines, 4, t)
-    if work is not out:
-        out.copy_(work)
-    return winner
+    return packed
 
 
 def draw_lines_csr(out: torch.Tensor, lines, frame_offsets, max_val: float = 1.0,

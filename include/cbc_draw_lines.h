@@ -224,9 +224,13 @@ CBC_API int cbc_squared_loss_backward_f64(const double *image, const double *tar
  * winner (the line sequential std::max keeps: the smallest index among the lines whose
  * value equals the pixel; 0x7f7f7f7f where no line raised the pixel above zero).
  * out (overwritten, no need to clear), winner: n_frames * height * width each;
- * packed: the same number of uint64 scratch values that must be zero on entry and are
- * zero again on return.  Other arguments as cbc_draw_lines_f32 (lines strategy).  With
- * cbc_draw_lines_backward_ex_* (winner_known = 1) the adjoint skips its winner pass.
+ * packed: the same number of uint64 values that must be zero on entry and are zero
+ * again on return.  With out = winner = NULL the call leaves packed holding, per
+ * pixel, (value bits << 32) | (0xffffffff - winner) (0 where no line raised the pixel)
+ * for cbc_draw_lines_backward_ex_f32, and the caller clears it before the next call.
+ * Other arguments as cbc_draw_lines_f32 (lines strategy).  With
+ * cbc_draw_lines_backward_ex_* (winner_known = 1, or packed) the adjoint skips its
+ * winner pass.
  * No counterpart in the reference (new). */
 CBC_API int cbc_draw_lines_max_winner_f32(float *out, int32_t *winner, uint64_t *packed,
                                           int64_t n_frames, int64_t height, int64_t width,
@@ -239,16 +243,19 @@ CBC_API int cbc_draw_lines_max_winner_f32(float *out, int32_t *winner, uint64_t 
 /* cbc_draw_lines_backward_* generalised: grad_out NULL takes the squared loss
  * sum((image - target)^2) (as cbc_squared_loss_backward_*); winner_known = 1 uses
  * `winner` as filled by cbc_draw_lines_max_winner_f32 instead of recomputing it (max
- * overlap, frames that started at zero).  No counterpart in the reference (new). */
+ * overlap, frames that started at zero); packed (float32 max overlap) takes image and
+ * winners from the pairs cbc_draw_lines_max_winner_f32 left with out = winner = NULL.
+ * No counterpart in the reference (new). */
 CBC_API int cbc_draw_lines_backward_ex_f32(const float *grad_out, const float *target,
                                            int64_t n_frames, int64_t height, int64_t width,
                                            const float *lines, int64_t n_lines,
                                            const void *idxs, int32_t idx_bytes, float max_val,
                                            int32_t kernel, int32_t overlap, const float *image,
                                            const float *out0, int32_t *winner,
-                                           int32_t winner_known, float *grad_lines,
-                                           void *workspace, size_t workspace_bytes,
-                                           int64_t checkpoint_capacity, void *stream);
+                                           int32_t winner_known, const uint64_t *packed,
+                                           float *grad_lines, void *workspace,
+                                           size_t workspace_bytes, int64_t checkpoint_capacity,
+                                           void *stream);
 
 CBC_API int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double *target,
                                            int64_t n_frames, int64_t height, int64_t width,
@@ -256,9 +263,10 @@ CBC_API int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double 
                                            const void *idxs, int32_t idx_bytes, double max_val,
                                            int32_t kernel, int32_t overlap, const double *image,
                                            const double *out0, int32_t *winner,
-                                           int32_t winner_known, double *grad_lines,
-                                           void *workspace, size_t workspace_bytes,
-                                           int64_t checkpoint_capacity, void *stream);
+                                           int32_t winner_known, const uint64_t *packed,
+                                           double *grad_lines, void *workspace,
+                                           size_t workspace_bytes, int64_t checkpoint_capacity,
+                                           void *stream);
 
 /* accumulate_lines for 2-D lines.  Replaces bresenham.accumulate_lines
  * (_src/src/bresenham.cpp:301-327, accumulate_lines_nd_impl :151-259) and

@@ -51,6 +51,9 @@ def test_fused_squared_loss_gradient_matches_autograd(cuda, overlap):
     else:                   # sum overlap: addition order differs between two renders
         torch.testing.assert_close(image, img.detach(), rtol=1e-5, atol=1e-4)
     torch.testing.assert_close(g, p.grad, rtol=1e-5, atol=1e-3)
+    if overlap == 'max':           # values and winners packed in one word, no frames
+        g2 = fit.squared_loss_step(None, target, lines, idxs, ls.max_val, ls.kernel, overlap)
+        torch.testing.assert_close(g2, g, rtol=1e-5, atol=1e-3)
 
 
 def test_fit_fused_and_autograd_paths_agree(cuda):
