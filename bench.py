@@ -61,6 +61,7 @@ def parse():
                         'biweight lines, max overlap')
     args = p.parse_args()
     args.steps_given = any(a == '--steps' or a.startswith('--steps=') for a in sys.argv[1:])
+    args.frames_given = any(a == '--frames' or a.startswith('--frames=') for a in sys.argv[1:])
     return args
 
 
@@ -361,7 +362,8 @@ def run_fit_loop(args, world, rank, local):
     import torch
     from cbclib_v2_gb300 import draw_lines, fit, workloads
     torch.cuda.set_device(local)
-    ls = workloads.fit_loop_stack(seed=4000 + rank)
+    frames = args.frames if args.frames_given else 32
+    ls = workloads.fit_loop_stack(seed=4000 + rank, F=frames)
     dev = torch.device('cuda', local)
     truth = torch.from_numpy(ls.lines.astype(np.float32)).to(dev)
     idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)

@@ -59,7 +59,8 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_accumulate_lines_3d_workspace_size', 'cbc_accumulate_lines_3d_f32',
            'cbc_accumulate_lines_3d_f64', 'cbc_squared_loss_backward_f32',
            'cbc_squared_loss_backward_f64', 'cbc_draw_lines_max_winner_f32',
-           'cbc_draw_lines_backward_ex_f32', 'cbc_draw_lines_backward_ex_f64')
+           'cbc_draw_lines_backward_ex_f32', 'cbc_draw_lines_backward_ex_f64',
+           'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32')
 
 NO_WINNER = 0x7f7f7f7f
 
@@ -126,6 +127,11 @@ def _declare(lib):
         f.argtypes = [p, p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, p, p, i32, p, p,
                       p, ctypes.c_size_t, i64, p]
         f.restype = ctypes.c_int
+    lib.cbc_squared_loss_step_workspace_size.argtypes = [i64, i64, i64, i64, i64, i64]
+    lib.cbc_squared_loss_step_workspace_size.restype = ctypes.c_size_t
+    lib.cbc_squared_loss_step_f32.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
+                                              i32, p, p, p, p, ctypes.c_size_t, i64, i64, p]
+    lib.cbc_squared_loss_step_f32.restype = ctypes.c_int
     lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
     lib.cbc_read_status.restype = ctypes.c_int
     lib.cbc_profile_enable.argtypes = [i32]

@@ -11,12 +11,15 @@
  * (biweight -3.75 (1 - x^2) / w^2, gaussian -9 K(x) / w^2, parabolic -1.5 / w^2;
  * rectangular 0; triangular -1 / (d w), taken as 0 at d = 0).
  *
- * The pixels are exactly the forward's: drive_segments (cbc_common.cuh) enumerates the
- * walk with the reference's arithmetic.  For max overlap a first pass records, per
- * pixel, the smallest line index whose exact value equals the final pixel value (and
- * exceeds the value before drawing): sequential std::max keeps the first such line,
- * so only that line receives the pixel's gradient.  Per-line sums are accumulated per
- * segment in shared memory, then in double in global memory.
+ * The pixels are exactly the forward's.  Sum overlap: drive_segments (cbc_common.cuh)
+ * enumerates every line's walk again with the reference's arithmetic and adds each
+ * drawn pixel's term; per-line sums are kept per segment in shared memory, then in
+ * double in global memory.  Max overlap: a pixel's gradient goes to one line, the
+ * smallest line index whose exact value equals the final pixel value (and exceeds the
+ * value before drawing; sequential std::max keeps the first such line).  Those
+ * winners come from the forward (cbc_draw_lines_max_winner_f32) or from a walk pass
+ * that recomputes them, and the gradient is then one streaming pass over the pixels
+ * (dense_max_kernel) that adds each pixel's term to its winner's sums.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -73,17 +76,14 @@ __device__ __forceinline__ T kappa_of(T d, T w, T max_val)
     }
 }
 
-template <typename T, int K, int OV>
+/* sum overlap: every drawn pixel (error <= 1) of every line gets its term */
+template <typename T, int K>
 struct BackwardAct {
     static constexpr bool kNeedsGeometry = true;
-    /* max overlap: a pixel whose winner is this line was drawn by it, so the error is
-     * not needed; sum overlap: every drawn pixel (error <= 1) */
-    static constexpr bool kNeedsError = OV != CBC_MAX;
+    static constexpr bool kNeedsError = true;
     const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
     const T *image;
     const T *target;
-    const unsigned long long *packed;   /* max overlap: (value bits, ~winner) per pixel */
-    const int *winner;   /* max overlap */
     double *gacc;        /* (N, 5) */
     T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
     T max_val;
@@ -101,36 +101,18 @@ struct BackwardAct {
             if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
         }
     }
-    /* max overlap: the winner first, the gradient only for the winning line; sum: the
-     * gradient of every pixel */
     struct Pre {
-        int win;
         T g;
     };
-    __device__ __forceinline__ T grad_at(long long at) const {
-        return grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
-    }
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
         const long long at = S.fbase[slot] + (long long)py * W + px;
         Pre p;
-        if (OV == CBC_MAX && packed) {
-            /* value and winner in one load, the target beside it: the squared-loss
-             * gradient of the winning line needs no second round trip */
-            const unsigned long long k = packed[at];
-            const unsigned hi = (unsigned)(k >> 32);
-            p.win = hi ? (int)(0xffffffffu - (unsigned)k) : 0x7f7f7f7f;
-            p.g = target ? T(2) * ((T)__uint_as_float(hi) - target[at]) : T(0);
-        } else {
-            p.win = OV == CBC_MAX ? winner[at] : 0;
-            p.g = OV == CBC_MAX ? T(0) : grad_at(at);
-        }
+        p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
         return p;
     }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
                                           T, const Pre &p) {
-        if (OV == CBC_MAX && p.win != S.line[slot]) return;
-        const T g = (OV == CBC_MAX && !(packed && target))
-                        ? grad_at(S.fbase[slot] + (long long)py * W + px) : p.g;
+        const T g = p.g;
         if (g == T(0)) return;
         const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
         const T w = S.w[slot];
@@ -153,6 +135,485 @@ struct BackwardAct {
     }
 };
 
+/* ---- max overlap: the adjoint as one pass over the pixels ----
+ * Under max overlap a drawn pixel's value comes from one line, its winner, so its
+ * adjoint is one line's term.  Rather than walking every line again and testing each
+ * pixel's winner, the pass streams the winners (or the forward's packed (value,
+ * winner) words) and dL/dI over the frames once, with 16-byte loads, and adds each
+ * drawn pixel's term to its winner's sums.
+ *
+ * The frames are read as a flat array of 8-pixel chunks.  A thread takes a patch of
+ * kPatchRows chunks one pitch apart, the pitch being W / 8 chunks rounded, so the
+ * chunks of a patch lie one below the other (sheared by at most 4 pixels per row) and
+ * neighbouring threads read neighbouring chunks.  A chunk row of a warp (32 chunks)
+ * has ~40 % drawn pixels, so rather than evaluating its 256 pixel positions with most
+ * lanes idle the warp compacts the drawn ones into a shared-memory queue and each lane
+ * evaluates a contiguous run of about total / 32 of them.  A lane keeps the sums of
+ * the two lines it met last in registers and flushes a line's sums to the double
+ * accumulators only when it makes room for another line, so a line reaches global
+ * memory a few times per patch row rather than once per pixel.  The per-line
+ * constants come from a table that one thread per line fills first
+ * (grad_coef_kernel). */
+constexpr int kChunk = 8;
+constexpr int kPatchRows = 8;
+constexpr int kDenseThreads = 256;
+
+enum : int { kSrcPacked = 0, kSrcWinner = 1 };
+
+/* per-line constants of the pixel terms.  With c = (cx, cy) the segment centre,
+ * tau = (t0, t1) = p1 - p0 and rmag = 1 / |tau|^2, the nearest point of the segment
+ * to pixel P is c + t tau, t = (P - c) . tau rmag clamped to [-1/2, 1/2]; with d the
+ * distance to it, kappa(d^2) is k0 + k1 d^2 (biweight, parabolic), k0 exp(k1 d^2)
+ * (gaussian), k0 / d (triangular, 0 at d = 0) or 0 (rectangular); rw = 1 / w. */
+template <typename T>
+struct alignas(8 * sizeof(T)) GradCoef {
+    T cx, cy, t0, t1, rmag, k0, k1, rw;
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(256)
+grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
+                 GradCoef<T> *__restrict__ coef)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T *ln = lines + i * 5;
+    const T x0 = ln[0], y0 = ln[1], x1 = ln[2], y1 = ln[3], w = ln[4];
+    GradCoef<T> c;
+    c.t0 = x1 - x0;
+    c.t1 = y1 - y0;
+    c.cx = x0 + T(0.5) * c.t0;
+    c.cy = y0 + T(0.5) * c.t1;
+    c.rmag = T(1) / (c.t0 * c.t0 + c.t1 * c.t1);
+    c.rw = T(1) / w;
+    const T rww = c.rw * c.rw;
+    switch (K) {
+    case CBC_BIWEIGHT:
+        c.k0 = T(-3.75) * max_val * rww;
+        c.k1 = -c.k0 * rww;
+        break;
+    case CBC_GAUSSIAN:
+        c.k0 = T(-9) * T(CBC_GAUSS_C) * max_val * rww;
+        c.k1 = T(-4.5) * rww;
+        break;
+    case CBC_PARABOLIC:
+        c.k0 = T(-1.5) * max_val * rww;
+        c.k1 = T(0);
+        break;
+    case CBC_RECTANGULAR:
+        c.k0 = c.k1 = T(0);
+        break;
+    default:
+        c.k0 = -max_val * c.rw;
+        c.k1 = T(0);
+        break;
+    }
+    coef[i] = c;
+}
+
+template <typename T, int K>
+__device__ __forceinline__ T kappa_d2(T d2, T k0, T k1)
+{
+    switch (K) {
+    case CBC_BIWEIGHT:  return k0 + k1 * d2;
+    case CBC_GAUSSIAN:  return k0 * exp(k1 * d2);
+    case CBC_PARABOLIC: return k0;
+    case CBC_RECTANGULAR: return T(0);
+    default: {
+        const T d = sqrt(d2);
+        return d > T(0) ? k0 / d : T(0);
+    }
+    }
+}
+
+/* g * dv/dtheta of one line at pixel (X, Y): v[0..4] for x0, y0, x1, y1, w */
+template <typename T, int K>
+__device__ __forceinline__ void pixel_term(const GradCoef<T> &c, T g, T X, T Y, T (&v)[5])
+{
+    T t = ((X - c.cx) * c.t0 + (Y - c.cy) * c.t1) * c.rmag;
+    t = t < T(-0.5) ? T(-0.5) : (t > T(0.5) ? T(0.5) : t);
+    const T dx = c.cx + t * c.t0 - X, dy = c.cy + t * c.t1 - Y;
+    const T d2 = dx * dx + dy * dy;
+    const T G = g * kappa_d2<T, K>(d2, c.k0, c.k1);
+    const T gb = G * (t + T(0.5)), ga = G - gb;
+    v[0] = ga * dx;
+    v[1] = ga * dy;
+    v[2] = gb * dx;
+    v[3] = gb * dy;
+    v[4] = -G * d2 * c.rw;
+}
+
+template <typename T>
+struct DenseArgs {
+    const unsigned long long *packed;   /* kSrcPacked: (value bits << 32) | ~line, 0: undrawn */
+    unsigned long long *clear;          /* kSrcPacked: zero the words after reading, or NULL */
+    const int *winner;                  /* kSrcWinner: line index, outside [0, N): none */
+    const T *grad_out;                  /* dL/dI, or NULL: 2 (I - target) */
+    const T *image;                     /* kSrcWinner without grad_out */
+    const T *target;
+    const GradCoef<T> *coef;            /* (N) */
+    double *gacc;                       /* (N, 5) sums */
+    double *partials;                   /* kSrcPacked: per-block sum of I (I - 2 T) over
+                                           drawn pixels, or NULL */
+    const DevStatus *st;                /* the forward's status (fatal: no gradient), or NULL */
+    unsigned long long *tasks;          /* task counter, zero at launch */
+    long long n_px, n_chunks, n_items;
+    int n_lines, H, W, pitch;
+    int vec;                            /* every base pointer is 16-byte aligned */
+};
+
+/* 8 elements from p + p0: two or four 16-byte loads when aligned and in range */
+template <typename U>
+__device__ __forceinline__ void load_chunk(const U *p, long long p0, long long n, bool vec,
+                                           U (&v)[kChunk])
+{
+    if (vec && p0 + kChunk <= n) {
+        constexpr int kQ = kChunk * (int)sizeof(U) / 16;
+        uint4 q[kQ];
+        const uint4 *src = reinterpret_cast<const uint4 *>(p + p0);
+        #pragma unroll
+        for (int i = 0; i < kQ; i++) q[i] = src[i];
+        __builtin_memcpy(v, q, sizeof(v));
+    } else {
+        #pragma unroll
+        for (int e = 0; e < kChunk; e++) v[e] = p0 + e < n ? p[p0 + e] : U(0);
+    }
+}
+
+/* a line's running sums with its constants */
+template <typename T>
+struct GradSlot {
+    int id;
+    GradCoef<T> c;
+    T s[5];
+    __device__ __forceinline__ void open(const GradCoef<T> *coef, int line) {
+        id = line;
+        c = coef[line];
+        #pragma unroll
+        for (int k = 0; k < 5; k++) s[k] = T(0);
+    }
+    __device__ __forceinline__ void flush(double *gacc) const {
+        if (id < 0) return;
+        double *g = gacc + (size_t)id * 5;
+        #pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (s[k] != T(0)) atomicAdd(g + k, (double)s[k]);
+    }
+};
+
+/* two lines' running sums, the least recently used one making room for a new line */
+template <typename T>
+struct SlotPair {
+    GradSlot<T> A, B;
+    bool mru_a;
+    template <int K>
+    __device__ __forceinline__ void add(const DenseArgs<T> &a, int line, T g, T X, T Y) {
+        bool in_a = line == A.id;
+        if (!in_a && line != B.id) {
+            if (mru_a) {
+                B.flush(a.gacc);
+                B.open(a.coef, line);
+            } else {
+                A.flush(a.gacc);
+                A.open(a.coef, line);
+                in_a = true;
+            }
+        }
+        mru_a = in_a;
+        GradCoef<T> c;
+        c.cx = in_a ? A.c.cx : B.c.cx;
+        c.cy = in_a ? A.c.cy : B.c.cy;
+        c.t0 = in_a ? A.c.t0 : B.c.t0;
+        c.t1 = in_a ? A.c.t1 : B.c.t1;
+        c.rmag = in_a ? A.c.rmag : B.c.rmag;
+        c.k0 = in_a ? A.c.k0 : B.c.k0;
+        c.k1 = in_a ? A.c.k1 : B.c.k1;
+        c.rw = in_a ? A.c.rw : B.c.rw;
+        T v[5];
+        pixel_term<T, K>(c, g, X, Y, v);
+        #pragma unroll
+        for (int k = 0; k < 5; k++) {
+            if (in_a) A.s[k] += v[k];
+            else B.s[k] += v[k];
+        }
+    }
+};
+
+/* advance pixel coordinates (x, y) by n >= 0 pixels of a W x H frame */
+__device__ __forceinline__ void advance_px(int &x, int &y, int n, int W, int H)
+{
+    x += n;
+    while (x >= W) {
+        x -= W;
+        if (++y == H) y = 0;
+    }
+}
+
+/* the per-warp queue of one chunk row's drawn pixels (up to 32 x 8), padded by one
+ * entry per 32 so that lane l reading entry l * m + r hits distinct banks */
+constexpr int kDenseWarps = kDenseThreads / 32;
+constexpr int kQueue = 32 * kChunk + kChunk;
+constexpr int kDenseMaxBlocks = 2048;   /* persistent grid cap = loss partials */
+
+__device__ __forceinline__ int qslot(int i) { return i + (i >> 5); }
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_1()
+{
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
+/* staging of the packed pass: per warp, two buffers of a chunk row's packed words and
+ * targets, stored piece-major ([piece][lane] 16-byte pieces) so that each lane's
+ * 16-byte reads of its own chunk are conflict-free */
+constexpr int kPkPieces = kChunk * 8 / 16;
+constexpr int kTgPieces = kChunk * 4 / 16;
+struct PackedStage {
+    uint4 pk[kDenseWarps][2][kPkPieces][32];
+    uint4 tg[kDenseWarps][2][kTgPieces][32];
+};
+
+template <typename T>
+struct DenseQueueT {
+    int line[kDenseWarps][kQueue];
+    T g[kDenseWarps][kQueue];
+    unsigned char pos[kDenseWarps][kQueue];
+    int x[kDenseWarps][32], y[kDenseWarps][32];
+};
+
+template <typename T>
+__host__ __device__ constexpr size_t dense_stage_offset()
+{
+    return (sizeof(DenseQueueT<T>) + 15) / 16 * 16;
+}
+
+template <typename T, int SRC>
+constexpr size_t dense_smem()
+{
+    return SRC == kSrcPacked && sizeof(T) == 4 ? dense_stage_offset<T>() + sizeof(PackedStage)
+                                               : sizeof(DenseQueueT<T>);
+}
+
+/* start the copy of chunk cc's packed words and targets into stage buffer buf (plain
+ * loads for a chunk at the end of the frames or unaligned buffers) */
+__device__ __forceinline__ void stage_chunk(PackedStage &S, int wid, int lane, int buf,
+                                            long long cc, const DenseArgs<float> &a)
+{
+    if (cc < a.n_chunks) {
+        const long long p0 = cc * kChunk;
+        if (a.vec && p0 + kChunk <= a.n_px) {
+            const uint4 *gp = reinterpret_cast<const uint4 *>(a.packed + p0);
+            #pragma unroll
+            for (int j = 0; j < kPkPieces; j++) cp_async16(&S.pk[wid][buf][j][lane], gp + j);
+            const uint4 *gt = reinterpret_cast<const uint4 *>(a.target + p0);
+            #pragma unroll
+            for (int j = 0; j < kTgPieces; j++) cp_async16(&S.tg[wid][buf][j][lane], gt + j);
+        } else {
+            unsigned long long w[kChunk];
+            float t[kChunk];
+            #pragma unroll
+            for (int e = 0; e < kChunk; e++) {
+                const bool in = p0 + e < a.n_px;
+                w[e] = in ? a.packed[p0 + e] : 0ull;
+                t[e] = in ? a.target[p0 + e] : 0.0f;
+            }
+            uint4 q[kPkPieces], r[kTgPieces];
+            __builtin_memcpy(q, w, sizeof(w));
+            __builtin_memcpy(r, t, sizeof(t));
+            #pragma unroll
+            for (int j = 0; j < kPkPieces; j++) S.pk[wid][buf][j][lane] = q[j];
+            #pragma unroll
+            for (int j = 0; j < kTgPieces; j++) S.tg[wid][buf][j][lane] = r[j];
+        }
+    }
+    cp_async_commit();
+}
+
+/* Persistent: each warp takes tasks of 32 patches (one per lane) from a counter until
+ * none are left, so the warps end together whatever the drawn density. */
+template <typename T, int K, int SRC>
+__global__ void __launch_bounds__(kDenseThreads, 3)
+dense_max_kernel(DenseArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char dense_smem_raw[];
+    DenseQueueT<T> &Q = *reinterpret_cast<DenseQueueT<T> *>(dense_smem_raw);
+    PackedStage &S = *reinterpret_cast<PackedStage *>(dense_smem_raw + dense_stage_offset<T>());
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool grad = K != CBC_RECTANGULAR && !(a.st && (a.st->flags & kFatal));
+    SlotPair<T> sp;
+    sp.A.id = sp.B.id = -1;
+    sp.mru_a = false;
+    #pragma unroll
+    for (int k = 0; k < 5; k++) sp.A.s[k] = sp.B.s[k] = T(0);
+    T loss = T(0);
+    const long long n_tasks = (a.n_items + 31) / 32;
+    #pragma unroll 1
+    while (true) {
+        long long task = 0;
+        if (lane == 0) task = (long long)atomicAdd(a.tasks, 1ull);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= n_tasks) break;
+        const long long it = task * 32 + lane;
+        long long c = a.n_chunks;
+        int x = 0, y = 0;
+        if (it < a.n_items) {
+            const long long band = it / a.pitch;
+            c = band * kPatchRows * a.pitch + (it - band * a.pitch);
+            if (c < a.n_chunks) {
+                const long long rem = (c * kChunk) % ((long long)a.H * a.W);
+                y = (int)(rem / a.W);
+                x = (int)(rem - (long long)y * a.W);
+            }
+        }
+        if constexpr (SRC == kSrcPacked && sizeof(T) == 4)
+            stage_chunk(S, wid, lane, 0, c, a);
+        /* every lane of the warp takes part in each chunk row (the queue is shared) */
+        #pragma unroll 1
+        for (int k = 0; k < kPatchRows; k++, c += a.pitch) {
+            const bool live = c < a.n_chunks;
+            const long long p0 = c * kChunk;
+            if (k > 0 && live) advance_px(x, y, (a.pitch - 1) * kChunk, a.W, a.H);
+            unsigned drawn = 0;
+            int ln[kChunk];
+            T gv[kChunk];
+            #pragma unroll
+            for (int e = 0; e < kChunk; e++) {
+                ln[e] = -1;
+                gv[e] = T(0);
+            }
+            if constexpr (SRC == kSrcPacked && sizeof(T) == 4) {
+                /* the next chunk row's copy goes out before this row is read */
+                if (k + 1 < kPatchRows) stage_chunk(S, wid, lane, (k + 1) & 1, c + a.pitch, a);
+                else cp_async_commit();
+                cp_async_wait_1();
+                if (live) {
+                    const int buf = k & 1;
+                    unsigned long long wv[kChunk];
+                    float tv[kChunk];
+                    uint4 q[kPkPieces], r[kTgPieces];
+                    #pragma unroll
+                    for (int j = 0; j < kPkPieces; j++) q[j] = S.pk[wid][buf][j][lane];
+                    #pragma unroll
+                    for (int j = 0; j < kTgPieces; j++) r[j] = S.tg[wid][buf][j][lane];
+                    __builtin_memcpy(wv, q, sizeof(wv));
+                    __builtin_memcpy(tv, r, sizeof(tv));
+                    unsigned nz = 0;
+                    #pragma unroll
+                    for (int e = 0; e < kChunk; e++) {
+                        nz |= (wv[e] != 0ull ? 1u : 0u) << e;
+                        ln[e] = (int)(0xffffffffu - (unsigned)wv[e]);
+                        drawn |= (wv[e] != 0ull && (unsigned)ln[e] < (unsigned)a.n_lines ? 1u : 0u)
+                                 << e;
+                        const T v = (T)__uint_as_float((unsigned)(wv[e] >> 32));
+                        if (wv[e] != 0ull) loss += v * (v - T(2) * (T)tv[e]);
+                        gv[e] = T(2) * (v - (T)tv[e]);
+                    }
+                    if (nz && a.clear) {
+                        if (a.vec && p0 + kChunk <= a.n_px) {
+                            uint4 *dst = reinterpret_cast<uint4 *>(a.clear + p0);
+                            #pragma unroll
+                            for (int i = 0; i < kChunk / 2; i++) dst[i] = make_uint4(0, 0, 0, 0);
+                        } else {
+                            #pragma unroll
+                            for (int e = 0; e < kChunk; e++)
+                                if (wv[e]) a.clear[p0 + e] = 0ull;
+                        }
+                    }
+                }
+            } else if (live) {
+                load_chunk(a.winner, p0, a.n_px, a.vec, ln);
+                #pragma unroll
+                for (int e = 0; e < kChunk; e++)
+                    drawn |= ((unsigned)ln[e] < (unsigned)a.n_lines ? 1u : 0u) << e;
+                if (drawn && grad) {
+                    if (a.grad_out) {
+                        load_chunk(a.grad_out, p0, a.n_px, a.vec, gv);
+                    } else {
+                        T iv[kChunk], tv[kChunk];
+                        load_chunk(a.image, p0, a.n_px, a.vec, iv);
+                        load_chunk(a.target, p0, a.n_px, a.vec, tv);
+                        #pragma unroll
+                        for (int e = 0; e < kChunk; e++) gv[e] = T(2) * (iv[e] - tv[e]);
+                    }
+                }
+            }
+            /* the pixels with a term, compacted into the warp's queue in pixel order */
+            unsigned work = 0;
+            if (grad) {
+                #pragma unroll
+                for (int e = 0; e < kChunk; e++)
+                    work |= (((drawn >> e) & 1u) && gv[e] != T(0) ? 1u : 0u) << e;
+            }
+            const int cnt = __popc(work);
+            int incl = cnt;
+            #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (total > 0) {
+                const int off = incl - cnt;
+                Q.x[wid][lane] = x;
+                Q.y[wid][lane] = y;
+                #pragma unroll
+                for (int e = 0; e < kChunk; e++) {
+                    if ((work >> e) & 1u) {
+                        const int q = qslot(off + __popc(work & ((1u << e) - 1u)));
+                        Q.line[wid][q] = ln[e];
+                        Q.g[wid][q] = gv[e];
+                        Q.pos[wid][q] = (unsigned char)((lane << 3) | e);
+                    }
+                }
+                __syncwarp();
+                /* lane l takes the contiguous entries [l m, l m + m): neighbouring
+                 * pixels, mostly of one or two lines */
+                const int m = (total + 31) >> 5;
+                #pragma unroll 1
+                for (int r = 0; r < m; r++) {
+                    const int i = lane * m + r;
+                    if (i < total) {
+                        const int q = qslot(i);
+                        const int line = Q.line[wid][q];
+                        const T g = Q.g[wid][q];
+                        const int pos = Q.pos[wid][q];
+                        int xe = Q.x[wid][pos >> 3], ye = Q.y[wid][pos >> 3];
+                        advance_px(xe, ye, pos & 7, a.W, a.H);
+                        sp.template add<K>(a, line, g, (T)xe, (T)ye);
+                    }
+                }
+                __syncwarp();
+            }
+            if (live) advance_px(x, y, kChunk, a.W, a.H);
+        }
+    }
+    sp.A.flush(a.gacc);
+    sp.B.flush(a.gacc);
+    if (SRC == kSrcPacked && a.partials) {
+        __shared__ double red[kDenseWarps];
+        double l = (double)loss;
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+        if (lane == 0) red[wid] = l;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = 0.0;
+            for (int w = 0; w < kDenseWarps; w++) b += red[w];
+            a.partials[blockIdx.x] = b;
+        }
+    }
+}
+
 template <typename T>
 struct AdjArgs {
     DriveArgs<T> d;
@@ -160,7 +621,6 @@ struct AdjArgs {
     const T *image;
     const T *out0;
     const T *target;
-    const unsigned long long *packed;
     int *winner;
     double *gacc;
     T max_val;
@@ -180,17 +640,15 @@ winner_kernel(AdjArgs<T> a)
     drive_segments(a.d, act);
 }
 
-template <typename T, int K, int OV>
+template <typename T, int K>
 __global__ void __launch_bounds__(kSegWarps * 32)
 backward_kernel(AdjArgs<T> a)
 {
     __shared__ T acc_s[kSegWarps][32][5];
-    BackwardAct<T, K, OV> act;
+    BackwardAct<T, K> act;
     act.grad_out = a.grad_out;
     act.image = a.image;
     act.target = a.target;
-    act.packed = a.packed;
-    act.winner = a.winner;
     act.gacc = a.gacc;
     act.acc = acc_s[threadIdx.x >> 5];
     act.max_val = a.max_val;
@@ -198,18 +656,37 @@ backward_kernel(AdjArgs<T> a)
     drive_segments(a.d, act);
 }
 
+/* grad_lines = gacc in T; with partials, block 0 also sums the dense pass's per-block
+ * loss partials into *loss */
 template <typename T>
-__global__ void finalize_kernel(const double *gacc, T *grad_lines, long long n)
+__global__ void __launch_bounds__(256)
+finalize_kernel(const double *gacc, T *grad_lines, long long n, const double *partials,
+                int n_partials, double *loss)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) grad_lines[i] = (T)gacc[i];
+    if (loss && blockIdx.x == 0) {
+        __shared__ double red[8];
+        double v = 0.0;
+        for (int k = threadIdx.x; k < n_partials; k += blockDim.x) v += partials[k];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) b += red[w];
+            *loss = b;
+        }
+    }
 }
 
 struct AdjLayout {
-    size_t status, recs, cks, gacc, total;
+    size_t status, recs, cks, gacc, coef, total;
 };
 
-AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes, size_t ck_bytes)
+AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes, size_t ck_bytes,
+                     size_t coef_bytes)
 {
     auto up = [](size_t v) { return (v + 255) / 256 * 256; };
     AdjLayout L;
@@ -217,31 +694,106 @@ AdjLayout adj_layout(long long n_lines, long long ck_capacity, size_t rec_bytes,
     L.status = off; off = up(off + sizeof(DevStatus));
     L.recs = off;   off = up(off + rec_bytes * (size_t)n_lines);
     L.cks = off;    off = up(off + ck_bytes * (size_t)ck_capacity);
-    L.gacc = off;   off = up(off + sizeof(double) * 5 * (size_t)n_lines);
+    L.gacc = off;   off = up(off + sizeof(double) * (5 * (size_t)n_lines + 1));
+    L.coef = off;   off = up(off + coef_bytes * (size_t)n_lines);
     L.total = off;
     return L;
 }
 
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+/* thread items of a dense pass over n_px pixels of width W: patches of kPatchRows
+ * chunks, pitch chunks per row step */
+inline int dense_pitch(long long W)
+{
+    const long long p = (W + kChunk / 2) / kChunk;
+    return (int)(p < 1 ? 1 : p);
+}
+
+inline long long dense_items(long long n_px, long long W)
+{
+    const long long chunks = (n_px + kChunk - 1) / kChunk;
+    const long long band = (long long)kPatchRows * dense_pitch(W);
+    return (chunks + band - 1) / band * dense_pitch(W);
+}
+
+/* fills the sizes, pitch and alignment of a dense pass over n_frames x H x W pixels */
+template <typename T>
+void dense_shape(DenseArgs<T> &a, long long n_frames, long long H, long long W)
+{
+    a.H = (int)H;
+    a.W = (int)W;
+    a.n_px = n_frames * H * W;
+    a.n_chunks = (a.n_px + kChunk - 1) / kChunk;
+    a.pitch = dense_pitch(W);
+    a.n_items = dense_items(a.n_px, W);
+    a.vec = aligned16(a.packed) && aligned16(a.clear) && aligned16(a.winner) &&
+            aligned16(a.grad_out) && aligned16(a.image) && aligned16(a.target);
+}
+
+/* the coefficient table of the lines, then the persistent pass: as many blocks as
+ * fit on the GPU (at most kDenseMaxBlocks); *blocks = the grid (loss partials) */
+template <typename T, int K, int SRC>
+cudaError_t launch_dense_k(const DenseArgs<T> &a, const T *lines, T max_val, cudaStream_t s,
+                           int *blocks)
+{
+    GradCoef<T> *coef = const_cast<GradCoef<T> *>(a.coef);
+    if (a.n_lines > 0) {
+        grad_coef_kernel<T, K><<<(unsigned)((a.n_lines + 255) / 256), 256, 0, s>>>(
+            lines, a.n_lines, max_val, coef);
+        note_launches(1);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (blocks) *blocks = 0;
+    if (a.n_items < 1) return cudaSuccess;
+    auto fn = dense_max_kernel<T, K, SRC>;
+    constexpr size_t smem = dense_smem<T, SRC>();
+    static std::atomic<int> grid_cache[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int g = grid_cache[dev & 63].load(std::memory_order_relaxed);
+    if (g == 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kDenseThreads, smem);
+        g = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        if (g > kDenseMaxBlocks) g = kDenseMaxBlocks;
+        grid_cache[dev & 63].store(g, std::memory_order_relaxed);
+    }
+    const long long need = (a.n_items + kDenseThreads - 1) / kDenseThreads;
+    const int grid = need < g ? (int)need : g;
+    fn<<<grid, kDenseThreads, smem, s>>>(a);
+    note_launches(1);
+    if (blocks) *blocks = grid;
+    return cudaGetLastError();
+}
+
+template <typename T, int SRC>
+cudaError_t launch_dense(const DenseArgs<T> &a, const T *lines, T max_val, int kernel,
+                         cudaStream_t s, int *blocks = nullptr)
+{
+    switch (kernel) {
+    case CBC_BIWEIGHT:    return launch_dense_k<T, CBC_BIWEIGHT, SRC>(a, lines, max_val, s, blocks);
+    case CBC_GAUSSIAN:    return launch_dense_k<T, CBC_GAUSSIAN, SRC>(a, lines, max_val, s, blocks);
+    case CBC_PARABOLIC:   return launch_dense_k<T, CBC_PARABOLIC, SRC>(a, lines, max_val, s, blocks);
+    case CBC_RECTANGULAR: return launch_dense_k<T, CBC_RECTANGULAR, SRC>(a, lines, max_val, s, blocks);
+    default:              return launch_dense_k<T, CBC_TRIANGULAR, SRC>(a, lines, max_val, s, blocks);
+    }
+}
+
 template <typename T, int K>
-cudaError_t launch_adjoint(const AdjArgs<T> &aa, int overlap, bool winner_known, cudaStream_t s)
+cudaError_t launch_walks(const AdjArgs<T> &aa, int overlap, cudaStream_t s)
 {
     if (overlap == CBC_MAX) {
-        if (!winner_known) {
-            const unsigned grid = resident_grid(winner_kernel<T, K>, kSegWarps * 32);
-            winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
-            note_launches(1);
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return e;
-            e = cudaMemsetAsync(aa.d.work, 0, sizeof(unsigned long long), s);
-            if (e != cudaSuccess) return e;
-        }
-        backward_kernel<T, K, CBC_MAX><<<resident_grid(backward_kernel<T, K, CBC_MAX>,
-                                                       kSegWarps * 32),
-                                         kSegWarps * 32, 0, s>>>(aa);
+        const unsigned grid = resident_grid(winner_kernel<T, K>, kSegWarps * 32);
+        winner_kernel<T, K><<<grid, kSegWarps * 32, 0, s>>>(aa);
     } else {
-        backward_kernel<T, K, CBC_SUM><<<resident_grid(backward_kernel<T, K, CBC_SUM>,
-                                                       kSegWarps * 32),
-                                         kSegWarps * 32, 0, s>>>(aa);
+        backward_kernel<T, K><<<resident_grid(backward_kernel<T, K>, kSegWarps * 32),
+                                kSegWarps * 32, 0, s>>>(aa);
     }
     note_launches(1);
     return cudaGetLastError();
@@ -278,9 +830,10 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         return fail(CBC_ERR_INVALID, "null grad_out");
     if (overlap == CBC_MAX && n_lines > 0 && pixels && !packed && (!image || !winner))
         return fail(CBC_ERR_INVALID, "max overlap needs the forward image and a winner buffer");
-    if (packed && (overlap != CBC_MAX || sizeof(T) != sizeof(float)))
-        return fail(CBC_ERR_INVALID, "packed winners are for float32 max overlap");
-    AdjLayout L = adj_layout(n_lines, ck_capacity, sizeof(LineRec<T>), sizeof(Checkpoint<T>));
+    if (packed && (overlap != CBC_MAX || sizeof(T) != sizeof(float) || !target))
+        return fail(CBC_ERR_INVALID, "packed winners are for the float32 max-overlap squared loss");
+    AdjLayout L = adj_layout(n_lines, ck_capacity, sizeof(LineRec<T>), sizeof(Checkpoint<T>),
+                             sizeof(GradCoef<T>));
     if (!workspace || ws_bytes < L.total)
         return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
                                          std::to_string(L.total) + ")");
@@ -295,27 +848,29 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     if (n_lines == 0) return CBC_OK;
-    e = cudaMemsetAsync(gacc, 0, sizeof(double) * 5 * (size_t)n_lines, s);
+    /* the (N, 5) sums and, after them, the dense pass's task counter */
+    e = cudaMemsetAsync(gacc, 0, sizeof(double) * (5 * (size_t)n_lines + 1), s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    Geometry g;
-    g.H = (int)H;
-    g.W = (int)W;
-    g.tile_w = g.tile_h = 64;
-    g.tiles_x = g.tiles_y = 1;
-    const unsigned nb = (unsigned)((n_lines + 255) / 256);
-    if (idxs && idx_bytes == 8)
-        prep_kernel<T, int64_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                                recs, nullptr, cks, ck_capacity, st,
-                                                                nullptr);
-    else
-        prep_kernel<T, int32_t, false, true><<<nb, 256, 0, s>>>(lines, idxs, n_lines, n_frames, g,
-                                                                recs, nullptr, cks, ck_capacity, st,
-                                                                nullptr);
-    note_launches(1);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    if (pixels) {
-        if (overlap == CBC_MAX && !winner_known) {
+    /* the walks (sum overlap, and the winner pass of max overlap) need the line records
+     * and walk checkpoints; the dense max pass needs only the lines */
+    const bool walks = pixels && (overlap == CBC_SUM || !winner_known);
+    if (walks) {
+        Geometry g;
+        g.H = (int)H;
+        g.W = (int)W;
+        g.tile_w = g.tile_h = 64;
+        g.tiles_x = g.tiles_y = 1;
+        const unsigned nb = (unsigned)((n_lines + 255) / 256);
+        if (idxs && idx_bytes == 8)
+            prep_kernel<T, int64_t, false, true><<<nb, 256, 0, s>>>(
+                lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st, nullptr);
+        else
+            prep_kernel<T, int32_t, false, true><<<nb, 256, 0, s>>>(
+                lines, idxs, n_lines, n_frames, g, recs, nullptr, cks, ck_capacity, st, nullptr);
+        note_launches(1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        if (overlap == CBC_MAX) {
             e = cudaMemsetAsync(winner, 0x7f, sizeof(int) * (size_t)(n_frames * H * W), s);
             if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         }
@@ -330,24 +885,126 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.image = image;
         aa.out0 = out0;
         aa.target = target;
-        aa.packed = packed;
         aa.winner = winner;
         aa.gacc = gacc;
         aa.max_val = max_val;
         switch (kernel) {
-        case CBC_BIWEIGHT:    e = launch_adjoint<T, CBC_BIWEIGHT>(aa, overlap, winner_known, s); break;
-        case CBC_GAUSSIAN:    e = launch_adjoint<T, CBC_GAUSSIAN>(aa, overlap, winner_known, s); break;
-        case CBC_PARABOLIC:   e = launch_adjoint<T, CBC_PARABOLIC>(aa, overlap, winner_known, s); break;
-        case CBC_RECTANGULAR: e = launch_adjoint<T, CBC_RECTANGULAR>(aa, overlap, winner_known, s); break;
-        default:              e = launch_adjoint<T, CBC_TRIANGULAR>(aa, overlap, winner_known, s); break;
+        case CBC_BIWEIGHT:    e = launch_walks<T, CBC_BIWEIGHT>(aa, overlap, s); break;
+        case CBC_GAUSSIAN:    e = launch_walks<T, CBC_GAUSSIAN>(aa, overlap, s); break;
+        case CBC_PARABOLIC:   e = launch_walks<T, CBC_PARABOLIC>(aa, overlap, s); break;
+        case CBC_RECTANGULAR: e = launch_walks<T, CBC_RECTANGULAR>(aa, overlap, s); break;
+        default:              e = launch_walks<T, CBC_TRIANGULAR>(aa, overlap, s); break;
+        }
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (pixels && overlap == CBC_MAX) {
+        DenseArgs<T> da{};
+        da.packed = packed;
+        da.winner = winner;
+        da.grad_out = grad_out;
+        da.image = image;
+        da.target = target;
+        da.coef = reinterpret_cast<GradCoef<T> *>(ws + L.coef);
+        da.gacc = gacc;
+        da.tasks = reinterpret_cast<unsigned long long *>(gacc + 5 * n_lines);
+        da.st = walks ? st : nullptr;
+        da.n_lines = (int)n_lines;
+        dense_shape(da, n_frames, H, W);
+        if constexpr (sizeof(T) == 4) {
+            e = packed ? launch_dense<T, kSrcPacked>(da, lines, max_val, kernel, s)
+                       : launch_dense<T, kSrcWinner>(da, lines, max_val, kernel, s);
+        } else {
+            e = launch_dense<T, kSrcWinner>(da, lines, max_val, kernel, s);
         }
         if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     }
     const long long n5 = 5 * n_lines;
-    finalize_kernel<T><<<(unsigned)((n5 + 255) / 256), 256, 0, s>>>(gacc, grad_lines, n5);
+    finalize_kernel<T><<<(unsigned)((n5 + 255) / 256), 256, 0, s>>>(gacc, grad_lines, n5, nullptr,
+                                                                    0, nullptr);
     note_launches(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
+/* the step workspace: the forward's (lines strategy) followed by the (N, 5) sums, the
+ * lines' coefficient table and the dense pass's per-block loss partials */
+struct StepLayout {
+    size_t draw, gacc, coef, partials, total;
+};
+
+bool step_layout(long long n_frames, long long H, long long W, long long n_lines,
+                 long long capacity, long long ck_capacity, StepLayout &L)
+{
+    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+    cbc_tuning t{};
+    t.strategy = CBC_STRATEGY_LINES;
+    L.draw = cbc_draw_lines_workspace_size(n_frames, H, W, n_lines, capacity, ck_capacity, 4, &t);
+    if (L.draw == 0) return false;
+    size_t off = up(L.draw);
+    L.gacc = off;     off = up(off + sizeof(double) * (5 * (size_t)n_lines + 1));
+    L.coef = off;     off = up(off + sizeof(GradCoef<float>) * (size_t)n_lines);
+    L.partials = off; off = up(off + sizeof(double) * kDenseMaxBlocks);
+    L.total = off;
+    return true;
+}
+
+int loss_step_impl(const float *target, long long n_frames, long long H, long long W,
+                   const float *lines, long long n_lines, const void *idxs, int idx_bytes,
+                   float max_val, int kernel, unsigned long long *packed, float *grad_lines,
+                   double *loss, void *workspace, size_t ws_bytes, long long capacity,
+                   long long ck_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0 || capacity < 0 || ck_capacity < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    const bool pixels = n_frames * H * W > 0;
+    if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (pixels && (!target || !packed)) return fail(CBC_ERR_INVALID, "null target or packed");
+    StepLayout L;
+    if (!step_layout(n_frames, H, W, n_lines, capacity, ck_capacity, L))
+        return fail(CBC_ERR_INVALID, "invalid sizes");
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    /* the forward: value and winner packed per pixel, no frames written */
+    int rc = cbc_draw_lines_max_winner_f32(nullptr, nullptr, reinterpret_cast<uint64_t *>(packed),
+                                           n_frames, H, W, lines, n_lines, idxs, idx_bytes,
+                                           max_val, kernel, workspace, L.draw, capacity,
+                                           ck_capacity, stream);
+    if (rc != CBC_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double *gacc = reinterpret_cast<double *>(ws + L.gacc);
+    double *partials = reinterpret_cast<double *>(ws + L.partials);
+    cudaError_t e = cudaSuccess;
+    e = cudaMemsetAsync(gacc, 0, sizeof(double) * (5 * (size_t)n_lines + 1), s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    int blocks = 0;
+    if (pixels) {
+        DenseArgs<float> da{};
+        da.packed = packed;
+        da.clear = packed;
+        da.target = target;
+        da.coef = reinterpret_cast<GradCoef<float> *>(ws + L.coef);
+        da.gacc = gacc;
+        da.tasks = reinterpret_cast<unsigned long long *>(gacc + 5 * n_lines);
+        da.partials = loss ? partials : nullptr;
+        da.st = reinterpret_cast<const DevStatus *>(ws);   /* the forward's status block */
+        da.n_lines = (int)n_lines;
+        dense_shape(da, n_frames, H, W);
+        e = launch_dense<float, kSrcPacked>(da, lines, max_val, kernel, s, &blocks);
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const long long n5 = 5 * n_lines;
+    if (n5 > 0 || loss) {
+        const long long nb = n5 > 0 ? (n5 + 255) / 256 : 1;
+        finalize_kernel<float><<<(unsigned)nb, 256, 0, s>>>(gacc, grad_lines, n5, partials,
+                                                             blocks, loss);
+        note_launches(1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
     return CBC_OK;
 }
 
@@ -361,7 +1018,8 @@ size_t cbc_draw_lines_backward_workspace_size(int64_t n_lines, int64_t checkpoin
     if (n_lines < 0 || checkpoint_capacity < 0) return 0;
     size_t rec = elem_bytes == 8 ? sizeof(cbc::LineRec<double>) : sizeof(cbc::LineRec<float>);
     size_t ck = elem_bytes == 8 ? sizeof(cbc::Checkpoint<double>) : sizeof(cbc::Checkpoint<float>);
-    return cbc::adj_layout(n_lines, checkpoint_capacity, rec, ck).total;
+    size_t coef = elem_bytes == 8 ? sizeof(cbc::GradCoef<double>) : sizeof(cbc::GradCoef<float>);
+    return cbc::adj_layout(n_lines, checkpoint_capacity, rec, ck, coef).total;
 }
 
 int cbc_draw_lines_backward_f32(const float *grad_out, int64_t n_frames, int64_t height,
@@ -456,6 +1114,32 @@ int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double *target,
                                       grad_lines, workspace, workspace_bytes,
                                       checkpoint_capacity, stream, grad_out ? nullptr : target,
                                       winner_known != 0);
+}
+
+size_t cbc_squared_loss_step_workspace_size(int64_t n_frames, int64_t height, int64_t width,
+                                            int64_t n_lines, int64_t pair_capacity,
+                                            int64_t checkpoint_capacity)
+{
+    if (n_frames < 0 || height < 0 || width < 0 || n_lines < 0 || pair_capacity < 0 ||
+        checkpoint_capacity < 0)
+        return 0;
+    cbc::StepLayout L;
+    if (!cbc::step_layout(n_frames, height, width, n_lines, pair_capacity, checkpoint_capacity, L))
+        return 0;
+    return L.total;
+}
+
+int cbc_squared_loss_step_f32(const float *target, int64_t n_frames, int64_t height,
+                              int64_t width, const float *lines, int64_t n_lines,
+                              const void *idxs, int32_t idx_bytes, float max_val, int32_t kernel,
+                              uint64_t *packed, float *grad_lines, double *loss_delta,
+                              void *workspace, size_t workspace_bytes, int64_t pair_capacity,
+                              int64_t checkpoint_capacity, void *stream)
+{
+    return cbc::loss_step_impl(target, n_frames, height, width, lines, n_lines, idxs, idx_bytes,
+                               max_val, kernel, reinterpret_cast<unsigned long long *>(packed),
+                               grad_lines, loss_delta, workspace, workspace_bytes, pair_capacity,
+                               checkpoint_capacity, stream);
 }
 
 }  // extern "C"

@@ -14,8 +14,8 @@ from typing import List, Optional
 
 import torch
 
-from . import ndimage
-from .autograd import _backward, draw_lines_fn, squared_loss_backward
+from . import _native, ndimage
+from .autograd import draw_lines_fn, squared_loss_backward
 
 __all__ = ['FitResult', 'fit_lines', 'squared_loss_step']
 
@@ -26,6 +26,7 @@ class FitResult:
     steps: int
     seconds: float                       # wall time of the steps (synchronised)
     losses: List[float] = field(default_factory=list)   # loss before step 0 and after the last
+    history: Optional[List[float]] = None   # loss at the start of every step (fused max path)
 
     @property
     def ms_per_step(self) -> float:
@@ -38,24 +39,57 @@ def _loss(params, idxs, target, max_val, kernel, overlap):
     return ((img - target) ** 2).sum()
 
 
+def _packed_loss_step(target: torch.Tensor, lines, idxs, max_val: float, kernel: str,
+                      loss_delta: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """cbc_squared_loss_step_f32: forward into this thread's packed scratch, gradient
+    of sum((draw(lines) - target)^2), scratch zeroed again, in one library call.
+    ``loss_delta`` (a float64 CUDA scalar, or None) receives the loss minus
+    sum(target^2)."""
+    k, _ = ndimage._check_names(kernel, 'max')
+    if not (target.is_cuda and target.dtype == torch.float32):
+        raise TypeError("target must be a float32 CUDA tensor")
+    dev = target.device
+    F, H, W = ndimage._frames_of(target)
+    ln = ndimage._as_device_lines(lines, dev, torch.float32)
+    if ln.shape[1] != 5:
+        raise ValueError("the fused loss step takes 2-D lines (N, 5)")
+    n = ln.shape[0]
+    ix = ndimage._as_device_idxs(idxs, n, dev)
+    if ix is None and n and F != 1 and F != n:
+        raise ValueError(f"idxs has an incompatible size ({n} != {F})")
+    tg = target.contiguous()
+    grad = torch.empty((n, 5), dtype=torch.float32, device=dev)
+    lib = _native.lib()
+    loss_ptr = None if loss_delta is None else loss_delta.data_ptr()
+
+    def call(buf, capacity, ck_capacity, tref, stream):
+        packed = ndimage._packed_scratch(dev, F * H * W)
+        return lib.cbc_squared_loss_step_f32(
+            tg.data_ptr(), F, H, W, ln.data_ptr(), n, None if ix is None else ix.data_ptr(),
+            0 if ix is None else ix.element_size(), max_val, k, packed.data_ptr(),
+            grad.data_ptr(), loss_ptr, buf.data_ptr(), buf.numel(), capacity, ck_capacity,
+            stream)
+
+    ndimage._run_with_workspace(call, dev, F, H, W, n, 4, None,
+                                size_fn=lib.cbc_squared_loss_step_workspace_size)
+    return grad
+
+
 def squared_loss_step(image: Optional[torch.Tensor], target: torch.Tensor, lines: torch.Tensor,
                       idxs: Optional[torch.Tensor], max_val: float, kernel: str, overlap: str,
-                      winner: Optional[torch.Tensor] = None) -> torch.Tensor:
+                      winner: Optional[torch.Tensor] = None,
+                      loss_delta: Optional[torch.Tensor] = None) -> torch.Tensor:
     """Render ``lines`` into ``image`` (overwritten, frames start at zero) and return
     the (N, 5) gradient of sum((image - target)^2): one forward kernel sequence and the
     fused loss adjoint, with no full-frame gradient in memory.  With image None (float32
     max overlap) the forward keeps each pixel's value and winner packed in one scratch
-    word and the adjoint reads them from there; no frames are written."""
+    word, no frames are written, and the adjoint is one pass over those words and the
+    target; ``loss_delta`` (float64 CUDA scalar) then receives the loss minus
+    sum(target^2)."""
     if image is None:
         if overlap != 'max' or target.dtype != torch.float32:
             raise ValueError("image=None is for float32 max overlap")
-        packed = ndimage._max_winner(None, None, target.shape, target.device, lines, idxs,
-                                     max_val, kernel)
-        try:
-            return _backward(lines, idxs, max_val, kernel, overlap, target.shape, target.dtype,
-                             target.device, target=target, packed=packed)
-        finally:
-            packed.zero_()
+        return _packed_loss_step(target, lines, idxs, max_val, kernel, loss_delta)
     if overlap == 'max' and image.dtype == torch.float32:
         # the forward records the winners: no winner pass in the adjoint
         winner = ndimage.draw_lines_max_winner(image, lines, idxs, max_val, kernel, winner)
@@ -85,10 +119,15 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
     image = torch.empty_like(target) if fused and not packed_path else None
     winner = (torch.empty(target.shape, dtype=torch.int32, device=target.device)
               if fused and overlap == 'max' and not packed_path else None)
+    deltas = torch.zeros(steps, dtype=torch.float64, device=target.device) if packed_path \
+        else None
     torch.cuda.synchronize(target.device)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        if fused:
+    for i in range(steps):
+        if packed_path:
+            params.grad = _packed_loss_step(target, params.detach(), idxs, max_val, kernel,
+                                            deltas[i])
+        elif fused:
             params.grad = squared_loss_step(image, target, params.detach(), idxs, max_val,
                                             kernel, overlap, winner)
         else:
@@ -100,6 +139,10 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
             params[:, 4].clamp_(min=min_width)
     torch.cuda.synchronize(target.device)
     seconds = time.perf_counter() - t0
+    history = None
+    if deltas is not None:
+        t2 = float(target.double().pow(2).sum())
+        history = [t2 + d for d in deltas.tolist()]
     with torch.no_grad():
         last = float(_loss(params, idxs, target, max_val, kernel, overlap))
-    return FitResult(params.detach(), steps, seconds, [first, last])
+    return FitResult(params.detach(), steps, seconds, [first, last], history)

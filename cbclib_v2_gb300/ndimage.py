@@ -237,10 +237,12 @@ class _on_current_device:
 
 
 def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines: int,
-                        elem: int, tuning) -> None:
-    """Run `call(buf, nbytes, capacity, ck_capacity, tref, stream)` with this thread's
+                        elem: int, tuning, size_fn=None) -> None:
+    """Run `call(buf, capacity, ck_capacity, tref, stream)` with this thread's
     workspace, read the status, raise the reference's errors and repeat with a larger
-    workspace when the call reports that its pairs or checkpoints did not fit."""
+    workspace when the call reports that its pairs or checkpoints did not fit.
+    ``size_fn(F, H, W, n_lines, capacity, ck_capacity)`` sizes the workspace of calls
+    whose workspace starts with a draw_lines one (default: the draw_lines size)."""
     lib = _native.lib()
     with _on_current_device(dev):
         stream = _current_stream(dev)
@@ -249,14 +251,15 @@ def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines
         ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
         tref = None if tuning is None else ctypes_pointer(tuning)
         for _ in range(4):
-            size_key = (F, H, W, n_lines, capacity, ck_capacity, elem,
+            size_key = (size_fn, F, H, W, n_lines, capacity, ck_capacity, elem,
                         None if tuning is None else tuple(getattr(tuning, f) for f, _ in
                                                           _native.Tuning._fields_))
             if ws.size_key == size_key:
                 nbytes = ws.size_bytes
             else:
-                nbytes = lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity,
-                                                           ck_capacity, elem, tref)
+                nbytes = (size_fn(F, H, W, n_lines, capacity, ck_capacity) if size_fn else
+                          lib.cbc_draw_lines_workspace_size(F, H, W, n_lines, capacity,
+                                                            ck_capacity, elem, tref))
                 if nbytes == 0:
                     raise ValueError(_native.last_error() or "invalid sizes or tuning")
                 ws.size_key, ws.size_bytes = size_key, nbytes

@@ -268,6 +268,29 @@ CBC_API int cbc_draw_lines_backward_ex_f64(const double *grad_out, const double 
                                            size_t workspace_bytes, int64_t checkpoint_capacity,
                                            void *stream);
 
+/* One step of a float32 max-overlap least-squares streak fit in one call: the forward
+ * (cbc_draw_lines_max_winner_f32 into `packed`, no frames written), then the gradient
+ * of L = sum((draw(lines) - target)^2) with respect to the (N, 5) lines into
+ * grad_lines, in one pass over the packed words and the target that also zeroes
+ * `packed` for the next call.  `packed` holds n_frames * height * width zeroed
+ * uint64 on entry and is zero again on return.  loss_delta (device, may be NULL)
+ * receives sum over drawn pixels of I (I - 2 target), i.e. L - sum(target^2).
+ * The workspace (cbc_squared_loss_step_workspace_size) starts with the forward's, so
+ * cbc_read_status on it reports the forward's errors and capacity needs.
+ * No counterpart in the reference (new). */
+CBC_API size_t cbc_squared_loss_step_workspace_size(int64_t n_frames, int64_t height,
+                                                    int64_t width, int64_t n_lines,
+                                                    int64_t pair_capacity,
+                                                    int64_t checkpoint_capacity);
+
+CBC_API int cbc_squared_loss_step_f32(const float *target, int64_t n_frames, int64_t height,
+                                      int64_t width, const float *lines, int64_t n_lines,
+                                      const void *idxs, int32_t idx_bytes, float max_val,
+                                      int32_t kernel, uint64_t *packed, float *grad_lines,
+                                      double *loss_delta, void *workspace,
+                                      size_t workspace_bytes, int64_t pair_capacity,
+                                      int64_t checkpoint_capacity, void *stream);
+
 /* accumulate_lines for 2-D lines.  Replaces bresenham.accumulate_lines
  * (_src/src/bresenham.cpp:301-327, accumulate_lines_nd_impl :151-259) and
  * cuda_draw_lines.accumulate_lines (_src/src/cuda_draw_lines.cu:1049-1057, 1077-1095).

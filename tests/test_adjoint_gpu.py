@@ -103,13 +103,16 @@ def torch_profile(kernel, x):
     return 1 - x
 
 
+@pytest.mark.parametrize("overlap", ['sum', 'max'])
 @pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'parabolic', 'rectangular',
                                     'triangular'])
-def test_gradient_matches_torch_closed_form(cuda, kernel):
+def test_gradient_matches_torch_closed_form(cuda, kernel, overlap):
     """One line per frame: the adjoint equals torch autograd of max_val * K(d / w)
     (d: distance to the segment, tests/draw_line_test.py:154-167 with Lines.project)
     summed over the pixels the forward drew, for every profile (including the
-    gaussian, whose jump at the support edge defeats finite differences)."""
+    gaussian, whose jump at the support edge defeats finite differences).  With one
+    line per frame every drawn pixel's winner is that line, so max overlap (the pass
+    over the pixels' winners) gives the same gradient as sum overlap (the walks)."""
     rng = np.random.default_rng(50)
     lines = separated_lines(rng, 3, 1)
     shape = (3, 40, 40)
@@ -118,7 +121,7 @@ def test_gradient_matches_torch_closed_form(cuda, kernel):
     idxs = np.arange(3)
     max_val = 1.7
     target = torch.tensor(rng.random(shape) * 0.3, device='cuda')
-    got, img = adjoint_gradient(lines, idxs, shape, target.cpu().numpy(), kernel, 'sum',
+    got, img = adjoint_gradient(lines, idxs, shape, target.cpu().numpy(), kernel, overlap,
                                 max_val, torch.float64)
     if kernel == 'rectangular':
         assert np.all(got == 0)

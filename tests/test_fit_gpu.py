@@ -68,3 +68,54 @@ def test_fit_fused_and_autograd_paths_agree(cuda):
     b = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel, overlap='sum',
                       steps=20, fused=False)
     torch.testing.assert_close(a.lines, b.lines, rtol=1e-4, atol=1e-3)
+
+
+@pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'parabolic', 'rectangular',
+                                    'triangular'])
+@pytest.mark.parametrize("shape", [(3, 23, 37), (1, 64, 64), (2, 9, 5)])
+def test_packed_loss_step_matches_image_path(cuda, kernel, shape):
+    """cbc_squared_loss_step_f32 (forward into packed words, one pass over them and the
+    target): the gradient of the image + winner path, the loss minus sum(T^2), and the
+    packed scratch left zero; frame sizes that are not multiples of the 8-pixel chunk,
+    and a target whose address is not 16-byte aligned (element loads)."""
+    from cbclib_v2_gb300 import ndimage
+    F, H, W = shape
+    rng = np.random.default_rng(F * 1000 + H + W)
+    n = 12 * F
+    lines = np.empty((n, 5))
+    lines[:, 0] = rng.uniform(-3, W + 3, n)
+    lines[:, 1] = rng.uniform(-3, H + 3, n)
+    lines[:, 2] = lines[:, 0] + rng.uniform(-15, 15, n)
+    lines[:, 3] = lines[:, 1] + rng.uniform(-15, 15, n)
+    lines[:, 4] = rng.uniform(0.7, 4, n)
+    lines = torch.tensor(lines, dtype=torch.float32, device='cuda')
+    idxs = torch.tensor(np.repeat(np.arange(F), 12), dtype=torch.int32, device='cuda')
+    base = torch.rand(F * H * W + 1, device='cuda') * 3
+    for target in (base[:-1].view(shape), base[1:].view(shape)):
+        image = torch.empty(shape, device='cuda')
+        want = fit.squared_loss_step(image, target, lines, idxs, 1.4, kernel, 'max')
+        delta = torch.zeros((), dtype=torch.float64, device='cuda')
+        got = fit.squared_loss_step(None, target, lines, idxs, 1.4, kernel, 'max',
+                                    loss_delta=delta)
+        torch.testing.assert_close(got, want, rtol=1e-5, atol=1e-4)
+        loss = float(((image.double() - target.double()) ** 2).sum())
+        t2 = float((target.double() ** 2).sum())
+        assert abs(t2 + float(delta) - loss) <= 1e-6 * loss
+        assert int(ndimage._packed_scratch(target.device, F * H * W).count_nonzero()) == 0
+    if kernel == 'rectangular':
+        assert torch.all(got == 0)
+
+
+def test_fit_loss_history(cuda):
+    """the fused max path records the loss at the start of every step"""
+    ls = workloads.fit_loop_stack(seed=12, F=2, H=128, W=120, per_frame=30)
+    truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+    target = torch.zeros(ls.shape, device='cuda')
+    draw_lines(target, truth, idxs, ls.max_val, ls.kernel, 'max')
+    start = torch.from_numpy(workloads.perturbed(ls.lines, 13, 1.0, 0.3).astype(np.float32)).cuda()
+    res = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel,
+                        overlap='max', steps=30)
+    assert res.history is not None and len(res.history) == 30
+    assert abs(res.history[0] - res.losses[0]) <= 1e-6 * res.losses[0]
+    assert res.history[-1] < 0.5 * res.history[0]
