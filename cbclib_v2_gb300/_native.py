@@ -60,7 +60,8 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_accumulate_lines_3d_f64', 'cbc_squared_loss_backward_f32',
            'cbc_squared_loss_backward_f64', 'cbc_draw_lines_max_winner_f32',
            'cbc_draw_lines_backward_ex_f32', 'cbc_draw_lines_backward_ex_f64',
-           'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32')
+           'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32',
+           'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status')
 
 NO_WINNER = 0x7f7f7f7f
 
@@ -132,6 +133,12 @@ def _declare(lib):
     lib.cbc_squared_loss_step_f32.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
                                               i32, p, p, p, p, ctypes.c_size_t, i64, i64, p]
     lib.cbc_squared_loss_step_f32.restype = ctypes.c_int
+    lib.cbc_status_bytes.argtypes = []
+    lib.cbc_status_bytes.restype = ctypes.c_size_t
+    lib.cbc_copy_status_async.argtypes = [p, p, p]
+    lib.cbc_copy_status_async.restype = ctypes.c_int
+    lib.cbc_decode_status.argtypes = [p, ctypes.POINTER(Status)]
+    lib.cbc_decode_status.restype = ctypes.c_int
     lib.cbc_read_status.argtypes = [p, ctypes.POINTER(Status), p]
     lib.cbc_read_status.restype = ctypes.c_int
     lib.cbc_profile_enable.argtypes = [i32]

@@ -28,6 +28,7 @@
 #include <limits.h>
 #include <stdio.h>
 #include <string.h>
+#include <cstring>
 #include <string>
 #include <atomic>
 #include <mutex>
@@ -921,6 +922,34 @@ int cbc_read_status(const void *workspace, cbc_status *status, void *stream)
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     const cbc::DevStatus d = *dst;
+    status->flags = d.flags;
+    status->strategy = d.strategy;
+    status->bad_line = (int64_t)d.bad_line;
+    status->idx_min = d.idx_min;
+    status->idx_max = d.idx_max;
+    status->pairs_needed = (int64_t)d.pairs;
+    status->checkpoints_needed = (int64_t)d.cks;
+    return CBC_OK;
+}
+
+size_t cbc_status_bytes(void) { return sizeof(cbc::DevStatus); }
+
+int cbc_copy_status_async(const void *workspace, void *dst, void *stream)
+{
+    cbc::g_error.clear();
+    if (!workspace || !dst) return cbc::fail(CBC_ERR_INVALID, "null pointer");
+    cudaError_t e = cudaMemcpyAsync(dst, workspace, sizeof(cbc::DevStatus), cudaMemcpyDeviceToHost,
+                                    static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
+int cbc_decode_status(const void *src, cbc_status *status)
+{
+    cbc::g_error.clear();
+    if (!src || !status) return cbc::fail(CBC_ERR_INVALID, "null pointer");
+    cbc::DevStatus d;
+    std::memcpy(&d, src, sizeof d);
     status->flags = d.flags;
     status->strategy = d.strategy;
     status->bad_line = (int64_t)d.bad_line;

@@ -388,6 +388,16 @@ CBC_API int cbc_accumulate_lines_3d_f64(double *out, int64_t n_frames, int64_t d
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
 CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
 
+/* The same status without waiting: cbc_copy_status_async enqueues on `stream` a copy
+ * of the device status block (cbc_status_bytes() bytes) into host memory `dst`
+ * (page-locked for an asynchronous copy); once the stream has passed it,
+ * cbc_decode_status turns those bytes into *status.  For callers that run several
+ * calls on several streams and check them all at one synchronisation point.
+ * No counterpart in the reference (new). */
+CBC_API size_t cbc_status_bytes(void);
+CBC_API int cbc_copy_status_async(const void *workspace, void *dst, void *stream);
+CBC_API int cbc_decode_status(const void *src, cbc_status *status);
+
 /* Per-stage device time of the calls made while profiling is on, from CUDA events
  * recorded on each call's stream around its kernels (no effect on results). */
 typedef struct cbc_profile {
