@@ -43,7 +43,8 @@ struct AccumAct {
     unsigned long long mask;       /* table capacity - 1 (a power of two) */
     DevStatus *st;
     struct Pre {};
-    __device__ __forceinline__ void item_begin(int) {}
+    template <class ST>
+    __device__ __forceinline__ void item_begin(int, const ST &) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &, int, int, int) const { return {}; }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,

@@ -45,7 +45,8 @@ struct WinnerAct {
     struct Pre {
         T img, o;
     };
-    __device__ __forceinline__ void item_begin(int) {}
+    template <class ST>
+    __device__ __forceinline__ void item_begin(int, const ST &) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
         const long long at = S.fbase[slot] + (long long)py * W + px;
@@ -63,103 +64,6 @@ struct WinnerAct {
     }
 };
 
-template <typename T, int K>
-__device__ __forceinline__ T kappa_of(T d, T w, T max_val)
-{
-    const T x = d / w, ww = w * w;
-    switch (K) {
-    case CBC_BIWEIGHT:  return max_val * T(-3.75) * (T(1) - x * x) / ww;
-    case CBC_GAUSSIAN:  return max_val * T(-9) * T(CBC_GAUSS_C) * exp(T(-4.5) * x * x) / ww;
-    case CBC_PARABOLIC: return max_val * T(-1.5) / ww;
-    case CBC_RECTANGULAR: return T(0);
-    default:            return d > T(0) ? -max_val / (d * w) : T(0);
-    }
-}
-
-/* sum overlap: every drawn pixel (error <= 1) of every line gets its term */
-template <typename T, int K>
-struct BackwardAct {
-    static constexpr bool kNeedsGeometry = true;
-    static constexpr bool kNeedsError = true;
-    const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
-    const T *image;
-    const T *target;
-    double *gacc;        /* (N, 5) */
-    T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
-    T max_val;
-    int W;
-    __device__ __forceinline__ void item_begin(int lane) {
-        #pragma unroll
-        for (int k = 0; k < 5; k++) acc[lane][k] = T(0);
-    }
-    __device__ __forceinline__ void item_end(int lane, const SlotTable<T> &S) {
-        const int line = S.line[lane];
-        if (line < 0) return;
-        #pragma unroll
-        for (int k = 0; k < 5; k++) {
-            const T v = acc[lane][k];
-            if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
-        }
-    }
-    struct Pre {
-        T g;
-    };
-    __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
-        const long long at = S.fbase[slot] + (long long)py * W + px;
-        Pre p;
-        p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
-        return p;
-    }
-    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
-                                          T, const Pre &p) {
-        const T g = p.g;
-        if (g == T(0)) return;
-        const T x0 = S.x0[slot], y0 = S.y0[slot], t0 = S.t0[slot], t1 = S.t1[slot];
-        const T w = S.w[slot];
-        const T X = (T)px, Y = (T)py;
-        const T cx = x0 + T(0.5) * t0, cy = y0 + T(0.5) * t1;
-        const T mag = t0 * t0 + t1 * t1;
-        T t = ((X - cx) * t0 + (Y - cy) * t1) / mag;
-        t = t < T(-0.5) ? T(-0.5) : (t > T(0.5) ? T(0.5) : t);
-        const T dx = cx + t * t0 - X, dy = cy + t * t1 - Y;
-        const T d2 = dx * dx + dy * dy;
-        const T d = sqrt(d2);
-        const T G = g * kappa_of<T, K>(d, w, max_val);
-        if (G == T(0)) return;
-        const T s = t + T(0.5);
-        atomicAdd(&acc[slot][0], G * (T(1) - s) * dx);
-        atomicAdd(&acc[slot][1], G * (T(1) - s) * dy);
-        atomicAdd(&acc[slot][2], G * s * dx);
-        atomicAdd(&acc[slot][3], G * s * dy);
-        atomicAdd(&acc[slot][4], -G * d2 / w);
-    }
-};
-
-/* ---- max overlap: the adjoint as one pass over the pixels ----
- * Under max overlap a drawn pixel's value comes from one line, its winner, so its
- * adjoint is one line's term.  Rather than walking every line again and testing each
- * pixel's winner, the pass streams the winners (or the forward's packed (value,
- * winner) words) and dL/dI over the frames once, with 16-byte loads, and adds each
- * drawn pixel's term to its winner's sums.
- *
- * The frames are read as a flat array of 8-pixel chunks.  A thread takes a patch of
- * kPatchRows chunks one pitch apart, the pitch being W / 8 chunks rounded, so the
- * chunks of a patch lie one below the other (sheared by at most 4 pixels per row) and
- * neighbouring threads read neighbouring chunks.  A chunk row of a warp (32 chunks)
- * has ~40 % drawn pixels, so rather than evaluating its 256 pixel positions with most
- * lanes idle the warp compacts the drawn ones into a shared-memory queue and each lane
- * evaluates a contiguous run of about total / 32 of them.  A lane keeps the sums of
- * the two lines it met last in registers and flushes a line's sums to the double
- * accumulators only when it makes room for another line, so a line reaches global
- * memory a few times per patch row rather than once per pixel.  The per-line
- * constants come from a table that one thread per line fills first
- * (grad_coef_kernel). */
-constexpr int kChunk = 8;
-constexpr int kPatchRows = 8;
-constexpr int kDenseThreads = 256;
-
-enum : int { kSrcPacked = 0, kSrcWinner = 1 };
-
 /* per-line constants of the pixel terms.  With c = (cx, cy) the segment centre,
  * tau = (t0, t1) = p1 - p0 and rmag = 1 / |tau|^2, the nearest point of the segment
  * to pixel P is c + t tau, t = (P - c) . tau rmag clamped to [-1/2, 1/2]; with d the
@@ -170,21 +74,16 @@ struct alignas(8 * sizeof(T)) GradCoef {
     T cx, cy, t0, t1, rmag, k0, k1, rw;
 };
 
+/* the constants of a line from its start point, tangent and width */
 template <typename T, int K>
-__global__ void __launch_bounds__(256)
-grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
-                 GradCoef<T> *__restrict__ coef)
+__device__ __forceinline__ GradCoef<T> make_grad_coef(T x0, T y0, T t0, T t1, T w, T max_val)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const T *ln = lines + i * 5;
-    const T x0 = ln[0], y0 = ln[1], x1 = ln[2], y1 = ln[3], w = ln[4];
     GradCoef<T> c;
-    c.t0 = x1 - x0;
-    c.t1 = y1 - y0;
-    c.cx = x0 + T(0.5) * c.t0;
-    c.cy = y0 + T(0.5) * c.t1;
-    c.rmag = T(1) / (c.t0 * c.t0 + c.t1 * c.t1);
+    c.t0 = t0;
+    c.t1 = t1;
+    c.cx = x0 + T(0.5) * t0;
+    c.cy = y0 + T(0.5) * t1;
+    c.rmag = T(1) / (t0 * t0 + t1 * t1);
     c.rw = T(1) / w;
     const T rww = c.rw * c.rw;
     switch (K) {
@@ -208,7 +107,19 @@ grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
         c.k1 = T(0);
         break;
     }
-    coef[i] = c;
+    return c;
+}
+
+template <typename T, int K>
+__global__ void __launch_bounds__(256)
+grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
+                 GradCoef<T> *__restrict__ coef)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T *ln = lines + i * 5;
+    const T x0 = ln[0], y0 = ln[1];
+    coef[i] = make_grad_coef<T, K>(x0, y0, ln[2] - x0, ln[3] - y0, ln[4], max_val);
 }
 
 template <typename T, int K>
@@ -242,6 +153,81 @@ __device__ __forceinline__ void pixel_term(const GradCoef<T> &c, T g, T X, T Y, 
     v[3] = gb * dy;
     v[4] = -G * d2 * c.rw;
 }
+
+/* sum overlap: every drawn pixel (error <= 1) of every line gets its term */
+template <typename T, int K>
+struct BackwardAct {
+    static constexpr bool kNeedsGeometry = true;
+    static constexpr bool kNeedsError = true;
+    const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
+    const T *image;
+    const T *target;
+    double *gacc;        /* (N, 5) */
+    T (*acc)[5];         /* this warp's per-slot accumulators (shared memory) */
+    GradCoef<T> *coef;   /* this warp's per-slot term constants (shared memory) */
+    T max_val;
+    int W;
+    __device__ __forceinline__ void item_begin(int lane, const SlotTable<T> &S) {
+        #pragma unroll
+        for (int k = 0; k < 5; k++) acc[lane][k] = T(0);
+        if (S.line[lane] >= 0)
+            coef[lane] = make_grad_coef<T, K>(S.x0[lane], S.y0[lane], S.t0[lane], S.t1[lane],
+                                              S.w[lane], max_val);
+    }
+    __device__ __forceinline__ void item_end(int lane, const SlotTable<T> &S) {
+        const int line = S.line[lane];
+        if (line < 0) return;
+        #pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const T v = acc[lane][k];
+            if (v != T(0)) atomicAdd(gacc + (size_t)line * 5 + k, (double)v);
+        }
+    }
+    struct Pre {
+        T g;
+    };
+    __device__ __forceinline__ Pre prefetch(const SlotTable<T> &S, int slot, int px, int py) const {
+        const long long at = S.fbase[slot] + (long long)py * W + px;
+        Pre p;
+        p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
+        return p;
+    }
+    __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
+                                          T, const Pre &p) {
+        const T g = p.g;
+        if (g == T(0)) return;
+        T v[5];
+        pixel_term<T, K>(coef[slot], g, (T)px, (T)py, v);
+        #pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (v[k] != T(0)) atomicAdd(&acc[slot][k], v[k]);
+    }
+};
+
+/* ---- max overlap: the adjoint as one pass over the pixels ----
+ * Under max overlap a drawn pixel's value comes from one line, its winner, so its
+ * adjoint is one line's term.  Rather than walking every line again and testing each
+ * pixel's winner, the pass streams the winners (or the forward's packed (value,
+ * winner) words) and dL/dI over the frames once, with 16-byte loads, and adds each
+ * drawn pixel's term to its winner's sums.
+ *
+ * The frames are read as a flat array of 8-pixel chunks.  A thread takes a patch of
+ * kPatchRows chunks one pitch apart, the pitch being W / 8 chunks rounded, so the
+ * chunks of a patch lie one below the other (sheared by at most 4 pixels per row) and
+ * neighbouring threads read neighbouring chunks.  A chunk row of a warp (32 chunks)
+ * has ~40 % drawn pixels, so rather than evaluating its 256 pixel positions with most
+ * lanes idle the warp compacts the drawn ones into a shared-memory queue and each lane
+ * evaluates a contiguous run of about total / 32 of them.  A lane keeps the sums of
+ * the two lines it met last in registers and flushes a line's sums to the double
+ * accumulators only when it makes room for another line, so a line reaches global
+ * memory a few times per patch row rather than once per pixel.  The per-line
+ * constants come from a table that one thread per line fills first
+ * (grad_coef_kernel). */
+constexpr int kChunk = 8;
+constexpr int kPatchRows = 8;
+constexpr int kDenseThreads = 256;
+
+enum : int { kSrcPacked = 0, kSrcWinner = 1 };
 
 template <typename T>
 struct DenseArgs {
@@ -645,12 +631,14 @@ __global__ void __launch_bounds__(kSegWarps * 32)
 backward_kernel(AdjArgs<T> a)
 {
     __shared__ T acc_s[kSegWarps][32][5];
+    __shared__ GradCoef<T> coef_s[kSegWarps][32];
     BackwardAct<T, K> act;
     act.grad_out = a.grad_out;
     act.image = a.image;
     act.target = a.target;
     act.gacc = a.gacc;
     act.acc = acc_s[threadIdx.x >> 5];
+    act.coef = coef_s[threadIdx.x >> 5];
     act.max_val = a.max_val;
     act.W = a.d.W;
     drive_segments(a.d, act);

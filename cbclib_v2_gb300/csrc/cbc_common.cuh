@@ -803,7 +803,7 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
  * A span walk ends at its first step with |ne| >= threshold (the reference's loop
  * condition) or when it leaves the frame.  The walks stay sequential per lane, as in
  * the reference, while the expensive per-pixel work runs on full warps.
- * act.item_begin(lane) / act.item_end(lane, slots) bracket each warp item; an action
+ * act.item_begin(lane, slots) / act.item_end(lane, slots) bracket each warp item; an action
  * that reads the line geometry from the slot table sets kNeedsGeometry, one that needs
  * no error (and is handed every visited pixel) clears kNeedsError.  The forward,
  * the max-overlap winner pass and the adjoint are such actions. */
@@ -1001,7 +1001,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 cols = true;
             }
         }
-        act.item_begin(lane);
+        act.item_begin(lane, S);
         __syncwarp();
 
         int guard = 0;

@@ -317,7 +317,8 @@ struct ForwardAct {
     int W;
     const float *gtab;   /* gaussian table (shared-memory copy) */
     struct Pre {};
-    __device__ __forceinline__ void item_begin(int) {}
+    template <class ST>
+    __device__ __forceinline__ void item_begin(int, const ST &) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<T> &) {}
     __device__ __forceinline__ Pre prefetch(const SlotTable<T> &, int, int, int) const { return {}; }
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T E,
@@ -342,7 +343,8 @@ struct PackedMaxAct {
     int W;
     const float *gtab;
     struct Pre {};
-    __device__ __forceinline__ void item_begin(int) {}
+    template <class ST>
+    __device__ __forceinline__ void item_begin(int, const ST &) {}
     __device__ __forceinline__ void item_end(int, const SlotTable<float> &) {}
     __device__ __forceinline__ Pre prefetch(const SlotTable<float> &, int, int, int) const {
         return {};
