@@ -61,7 +61,8 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_squared_loss_backward_f64', 'cbc_draw_lines_max_winner_f32',
            'cbc_draw_lines_backward_ex_f32', 'cbc_draw_lines_backward_ex_f64',
            'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32',
-           'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status')
+           'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status',
+           'cbc_adam_step_f32')
 
 NO_WINNER = 0x7f7f7f7f
 
@@ -133,6 +134,9 @@ def _declare(lib):
     lib.cbc_squared_loss_step_f32.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
                                               i32, p, p, p, p, ctypes.c_size_t, i64, i64, p]
     lib.cbc_squared_loss_step_f32.restype = ctypes.c_int
+    lib.cbc_adam_step_f32.argtypes = [p, p, p, p, i64, i64, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_float, ctypes.c_float, p]
+    lib.cbc_adam_step_f32.restype = ctypes.c_int
     lib.cbc_status_bytes.argtypes = []
     lib.cbc_status_bytes.restype = ctypes.c_size_t
     lib.cbc_copy_status_async.argtypes = [p, p, p]

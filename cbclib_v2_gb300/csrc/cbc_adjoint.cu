@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <limits.h>
+#include <cmath>
 #include <string>
 
 #include "cbc_common.cuh"
@@ -996,9 +997,52 @@ int loss_step_impl(const float *target, long long n_frames, long long H, long lo
     return CBC_OK;
 }
 
+/* one Adam step on the (N, 5) line parameters with the width clamp:
+ * m = m + (1 - b1)(g - m), v = b2 v + (1 - b2) g^2,
+ * p -= (lr / (1 - b1^t)) m / (sqrt(v) / sqrt(1 - b2^t) + eps), widths >= min_width */
+__global__ void __launch_bounds__(256)
+adam_kernel(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+            float *__restrict__ v, long long n, float step_size, float bc2_sqrt, float b1,
+            float b2, float eps, float min_width)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = m[i] + (1.0f - b1) * (gi - m[i]);
+    const float vi = v[i] * b2 + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    float pi = p[i] - step_size * (mi / (sqrtf(vi) / bc2_sqrt + eps));
+    if (i % 5 == 4 && pi < min_width) pi = min_width;
+    p[i] = pi;
+}
+
 }  // namespace cbc
 
 extern "C" {
+
+int cbc_adam_step_f32(float *params, const float *grad, float *exp_avg, float *exp_avg_sq,
+                      int64_t n_lines, int64_t step, float lr, float beta1, float beta2,
+                      float eps, float min_width, void *stream)
+{
+    cbc::clear_error();
+    if (n_lines < 0 || step < 1) return cbc::fail(CBC_ERR_INVALID, "n_lines < 0 or step < 1");
+    if (!(beta1 >= 0.0f && beta1 < 1.0f && beta2 >= 0.0f && beta2 < 1.0f))
+        return cbc::fail(CBC_ERR_INVALID, "betas must lie in [0, 1)");
+    if (n_lines == 0) return CBC_OK;
+    if (!params || !grad || !exp_avg || !exp_avg_sq) return cbc::fail(CBC_ERR_INVALID, "null pointer");
+    const double bc1 = 1.0 - std::pow((double)beta1, (double)step);
+    const double bc2 = 1.0 - std::pow((double)beta2, (double)step);
+    const long long n = 5 * n_lines;
+    cbc::adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        params, grad, exp_avg, exp_avg_sq, n, (float)(lr / bc1), (float)std::sqrt(bc2), beta1,
+        beta2, eps, min_width);
+    cbc::note_launches(1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
 
 size_t cbc_draw_lines_backward_workspace_size(int64_t n_lines, int64_t checkpoint_capacity,
                                               int32_t elem_bytes)

@@ -17,7 +17,7 @@ import torch
 from . import _native, ndimage
 from .autograd import draw_lines_fn, squared_loss_backward
 
-__all__ = ['FitResult', 'fit_lines', 'squared_loss_step']
+__all__ = ['FitResult', 'adam_step', 'fit_lines', 'squared_loss_step']
 
 
 @dataclass
@@ -101,6 +101,26 @@ def squared_loss_step(image: Optional[torch.Tensor], target: torch.Tensor, lines
                                  winner=winner)
 
 
+def adam_step(params: torch.Tensor, grad: torch.Tensor, exp_avg: torch.Tensor,
+              exp_avg_sq: torch.Tensor, step: int, lr: float, betas=(0.9, 0.999),
+              eps: float = 1e-8, min_width: float = 0.0) -> None:
+    """One Adam step on contiguous float32 CUDA (N, 5) line parameters in place
+    (cbc_adam_step_f32: torch.optim.Adam's update, then widths >= min_width); exp_avg
+    and exp_avg_sq are the optimiser state (zeros before step 1)."""
+    ts = (params, grad, exp_avg, exp_avg_sq)
+    if not all(t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and
+               t.shape == params.shape for t in ts) or params.dim() != 2 or params.shape[1] != 5:
+        raise ValueError("adam_step takes contiguous float32 CUDA (N, 5) tensors")
+    lib = _native.lib()
+    with ndimage._on_current_device(params.device):
+        rc = lib.cbc_adam_step_f32(params.data_ptr(), grad.data_ptr(), exp_avg.data_ptr(),
+                                   exp_avg_sq.data_ptr(), params.shape[0], step, lr, betas[0],
+                                   betas[1], eps, min_width,
+                                   ndimage._current_stream(params.device))
+    if rc:
+        ndimage._raise_rc(rc)
+
+
 def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.Tensor] = None,
               *, max_val: float = 1.0, kernel: str = 'biweight', overlap: str = 'sum',
               steps: int = 100, lr: float = 0.05, min_width: float = 0.5,
@@ -112,7 +132,13 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
     if not target.is_cuda:
         raise ValueError("target must be a CUDA tensor")
     params = lines0.detach().to(target.device, target.dtype).clone().requires_grad_(True)
-    opt = torch.optim.Adam([params], lr=lr)
+    # the fused float32 paths update in one library kernel (cbc_adam_step_f32, torch's
+    # Adam formula with its default betas and eps); the others use torch.optim.Adam
+    native = fused and target.dtype == torch.float32
+    opt = None if native else torch.optim.Adam([params], lr=lr)
+    if native:
+        exp_avg = torch.zeros_like(params, memory_format=torch.contiguous_format)
+        exp_avg_sq = torch.zeros_like(exp_avg)
     with torch.no_grad():
         first = float(_loss(params, idxs, target, max_val, kernel, overlap))
     packed_path = fused and overlap == 'max' and target.dtype == torch.float32
@@ -134,9 +160,13 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
             loss = _loss(params, idxs, target, max_val, kernel, overlap)
             opt.zero_grad(set_to_none=True)
             loss.backward()
-        opt.step()
-        with torch.no_grad():
-            params[:, 4].clamp_(min=min_width)
+        if native:
+            adam_step(params.detach(), params.grad, exp_avg, exp_avg_sq, i + 1, lr,
+                      min_width=min_width)
+        else:
+            opt.step()
+            with torch.no_grad():
+                params[:, 4].clamp_(min=min_width)
     torch.cuda.synchronize(target.device)
     seconds = time.perf_counter() - t0
     history = None

@@ -291,6 +291,17 @@ CBC_API int cbc_squared_loss_step_f32(const float *target, int64_t n_frames, int
                                       size_t workspace_bytes, int64_t pair_capacity,
                                       int64_t checkpoint_capacity, void *stream);
 
+/* One Adam step on the (N, 5) float32 line parameters of a streak fit, in one kernel:
+ * exp_avg = exp_avg + (1 - beta1)(grad - exp_avg),
+ * exp_avg_sq = beta2 exp_avg_sq + (1 - beta2) grad^2,
+ * params -= lr / (1 - beta1^step) * exp_avg / (sqrt(exp_avg_sq) / sqrt(1 - beta2^step) + eps),
+ * then widths (column 4) are raised to min_width.  step counts from 1; the state
+ * starts at zero.  No counterpart in the reference (new). */
+CBC_API int cbc_adam_step_f32(float *params, const float *grad, float *exp_avg,
+                              float *exp_avg_sq, int64_t n_lines, int64_t step, float lr,
+                              float beta1, float beta2, float eps, float min_width,
+                              void *stream);
+
 /* accumulate_lines for 2-D lines.  Replaces bresenham.accumulate_lines
  * (_src/src/bresenham.cpp:301-327, accumulate_lines_nd_impl :151-259) and
  * cuda_draw_lines.accumulate_lines (_src/src/cuda_draw_lines.cu:1049-1057, 1077-1095).

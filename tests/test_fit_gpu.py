@@ -119,3 +119,24 @@ def test_fit_loss_history(cuda):
     assert res.history is not None and len(res.history) == 30
     assert abs(res.history[0] - res.losses[0]) <= 1e-6 * res.losses[0]
     assert res.history[-1] < 0.5 * res.history[0]
+
+
+def test_adam_step_matches_torch_adam(cuda):
+    """cbc_adam_step_f32 follows torch.optim.Adam (default betas, eps), then clamps the
+    widths"""
+    rng = np.random.default_rng(14)
+    p0 = torch.tensor(rng.normal(0, 3, (300, 5)), dtype=torch.float32, device='cuda')
+    p0[:, 4] = p0[:, 4].abs() + 0.6
+    a = p0.clone().requires_grad_(True)
+    opt = torch.optim.Adam([a], lr=0.05)
+    b = p0.clone()
+    m, v = torch.zeros_like(b), torch.zeros_like(b)
+    for step in range(1, 8):
+        g = torch.tensor(rng.normal(0, 10, (300, 5)), dtype=torch.float32, device='cuda')
+        a.grad = g.clone()
+        opt.step()
+        with torch.no_grad():
+            a[:, 4].clamp_(min=0.5)
+        fit.adam_step(b, g, m, v, step, 0.05, min_width=0.5)
+        torch.testing.assert_close(b, a.detach(), rtol=1e-6, atol=1e-6)
+    assert float(b[:, 4].min()) >= 0.5
