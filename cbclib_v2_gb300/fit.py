@@ -75,6 +75,64 @@ def _packed_loss_step(target: torch.Tensor, lines, idxs, max_val: float, kernel:
     return grad
 
 
+class _PackedSteps:
+    """The fused loss steps of one fit: the first step runs through the checking
+    path (which sizes the workspace), later steps enqueue the library call and an
+    asynchronous copy of its device status, read once after the last step."""
+
+    def __init__(self, target: torch.Tensor, idxs, max_val: float, kernel: str, n: int,
+                 steps: int):
+        self.k, _ = ndimage._check_names(kernel, 'max')
+        self.dev = target.device
+        self.F, self.H, self.W = ndimage._frames_of(target)
+        self.tg = target.contiguous()
+        self.ix = ndimage._as_device_idxs(idxs, n, self.dev)
+        self.n, self.max_val, self.kernel = n, max_val, kernel
+        self.lib = _native.lib()
+        nb = int(self.lib.cbc_status_bytes())
+        self.status = torch.zeros((max(steps, 1), nb), dtype=torch.uint8).pin_memory()
+        self.ws = None
+
+    def first(self, lines: torch.Tensor, delta: torch.Tensor) -> torch.Tensor:
+        grad = _packed_loss_step(self.tg, lines, self.ix, self.max_val, self.kernel, delta)
+        stream = ndimage._current_stream(self.dev)
+        ws = ndimage._workspace_raw(self.dev, stream)
+        need = ws.last_status.checkpoints_needed if ws.last_status is not None else 0
+        self.cap = ws.capacity
+        self.ck = max(ws.ck_capacity, 2 * need + 4096)     # room for the lines to move
+        nbytes = self.lib.cbc_squared_loss_step_workspace_size(self.F, self.H, self.W, self.n,
+                                                               self.cap, self.ck)
+        self.buf = ws.ensure(nbytes)
+        self.stream = stream
+        return grad
+
+    def enqueue(self, i: int, lines: torch.Tensor, grad: torch.Tensor,
+                delta: torch.Tensor) -> None:
+        packed = ndimage._packed_scratch(self.dev, self.F * self.H * self.W)
+        ix = self.ix
+        rc = self.lib.cbc_squared_loss_step_f32(
+            self.tg.data_ptr(), self.F, self.H, self.W, lines.data_ptr(), self.n,
+            None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+            self.max_val, self.k, packed.data_ptr(), grad.data_ptr(), delta.data_ptr(),
+            self.buf.data_ptr(), self.buf.numel(), self.cap, self.ck, self.stream)
+        if rc == 0:
+            rc = self.lib.cbc_copy_status_async(self.buf.data_ptr(), self.status[i].data_ptr(),
+                                                self.stream)
+        if rc:
+            ndimage._raise_rc(rc)
+
+    def failed(self, upto: int) -> bool:
+        """after a synchronisation: True if a step in [1, upto) ran out of walk
+        checkpoints (it drew nothing); other errors raise"""
+        capacity = False
+        for i in range(1, upto):
+            st = _native.Status()
+            self.lib.cbc_decode_status(self.status[i].data_ptr(), st)
+            capacity = capacity or st.has(_native.CBC_ERR_CAPACITY)
+            ndimage._raise_status(st, self.F)
+        return capacity
+
+
 def squared_loss_step(image: Optional[torch.Tensor], target: torch.Tensor, lines: torch.Tensor,
                       idxs: Optional[torch.Tensor], max_val: float, kernel: str, overlap: str,
                       winner: Optional[torch.Tensor] = None,
@@ -124,11 +182,16 @@ def adam_step(params: torch.Tensor, grad: torch.Tensor, exp_avg: torch.Tensor,
 def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.Tensor] = None,
               *, max_val: float = 1.0, kernel: str = 'biweight', overlap: str = 'sum',
               steps: int = 100, lr: float = 0.05, min_width: float = 0.5,
-              fused: bool = True) -> FitResult:
+              fused: bool = True, _checked: bool = False) -> FitResult:
     """Refine ``lines0`` (N, 5) so that draw_lines(lines) matches ``target`` (frames on
     the GPU), with ``steps`` Adam steps of learning rate ``lr``.  ``fused`` takes the
     gradient from the fused squared-loss adjoint (squared_loss_step); otherwise it goes
-    through torch autograd (draw_lines_fn and a torch loss), with the same result."""
+    through torch autograd (draw_lines_fn and a torch loss), with the same result.
+
+    On the float32 max-overlap path the steps after the first do not wait for the GPU:
+    their status is read after the last step, and if one of them ran out of walk
+    checkpoints (the lines grew far beyond the reserve) the whole fit runs again with a
+    check after every step."""
     if not target.is_cuda:
         raise ValueError("target must be a CUDA tensor")
     params = lines0.detach().to(target.device, target.dtype).clone().requires_grad_(True)
@@ -147,10 +210,16 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
               if fused and overlap == 'max' and not packed_path else None)
     deltas = torch.zeros(steps, dtype=torch.float64, device=target.device) if packed_path \
         else None
+    stepper = (_PackedSteps(target, idxs, max_val, kernel, params.shape[0], steps)
+               if packed_path and not _checked else None)
     torch.cuda.synchronize(target.device)
     t0 = time.perf_counter()
     for i in range(steps):
-        if packed_path:
+        if stepper is not None and i > 0:
+            stepper.enqueue(i, params.detach(), params.grad, deltas[i])
+        elif stepper is not None:
+            params.grad = stepper.first(params.detach(), deltas[i])
+        elif packed_path:
             params.grad = _packed_loss_step(target, params.detach(), idxs, max_val, kernel,
                                             deltas[i])
         elif fused:
@@ -169,6 +238,9 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
                 params[:, 4].clamp_(min=min_width)
     torch.cuda.synchronize(target.device)
     seconds = time.perf_counter() - t0
+    if stepper is not None and stepper.failed(steps):
+        return fit_lines(target, lines0, idxs, max_val=max_val, kernel=kernel, overlap=overlap,
+                         steps=steps, lr=lr, min_width=min_width, fused=fused, _checked=True)
     history = None
     if deltas is not None:
         t2 = float(target.double().pow(2).sum())

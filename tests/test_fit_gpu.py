@@ -140,3 +140,32 @@ def test_adam_step_matches_torch_adam(cuda):
         fit.adam_step(b, g, m, v, step, 0.05, min_width=0.5)
         torch.testing.assert_close(b, a.detach(), rtol=1e-6, atol=1e-6)
     assert float(b[:, 4].min()) >= 0.5
+
+
+def test_unchecked_steps_fall_back_when_checkpoints_run_out(cuda, monkeypatch):
+    """steps after the first read their status only at the end; a step that ran out of
+    walk checkpoints makes the whole fit run again with a check after every step"""
+    ls = workloads.fit_loop_stack(seed=15, F=2, H=128, W=120, per_frame=30)
+    truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+    target = torch.zeros(ls.shape, device='cuda')
+    draw_lines(target, truth, idxs, ls.max_val, ls.kernel, 'max')
+    start = torch.from_numpy(workloads.perturbed(ls.lines, 16, 1.0, 0.3).astype(np.float32)).cuda()
+    kw = dict(max_val=ls.max_val, kernel=ls.kernel, overlap='max', steps=12)
+    want = fit.fit_lines(target, start, idxs, _checked=True, **kw)
+    first = fit._PackedSteps.first
+    runs = []
+
+    def starved(self, lines, delta):
+        g = first(self, lines, delta)
+        self.ck = 1                        # no room: every later step overflows
+        runs.append(1)
+        return g
+
+    monkeypatch.setattr(fit._PackedSteps, 'first', starved)
+    got = fit.fit_lines(target, start, idxs, **kw)
+    assert len(runs) == 1
+    torch.testing.assert_close(got.lines, want.lines, rtol=1e-5, atol=1e-5)
+    monkeypatch.setattr(fit._PackedSteps, 'first', first)
+    again = fit.fit_lines(target, start, idxs, **kw)
+    torch.testing.assert_close(again.lines, want.lines, rtol=1e-5, atol=1e-5)
