@@ -7,8 +7,9 @@ indices): one step = one draw_lines call over the whole stack.
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput in Mlines/s
 (lines, indices and frames already in HBM); `e2e` is the same metric through the
-public API with pinned host buffers (frames, lines and indices copied in, frames
-copied out every step).  `roofline` is the dominant kernel's achieved HBM bandwidth
+public API with the frames, lines and indices in pinned host buffers: every step copies
+the lines and indices to the device, and the kernels combine the drawn pixels into the
+host frames in place through their device mapping (only drawn pixels cross the link).  `roofline` is the dominant kernel's achieved HBM bandwidth
 (segments_kernel or render_kernel, whichever strategy the call ran) from CUDA events
 recorded on its stream around every launch in the timed region.  Its byte count is the
 call's contract: draw_lines updates `out` in place, so every output pixel is read and
@@ -490,10 +491,20 @@ def main():
             tt = torch.tensor([e_ms], device=dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             e_ms = float(tt.item())
+        # the frames stay in page-locked host memory: the library's kernels read and
+        # write the drawn pixels there through their device mapping (NVLink-C2C), so
+        # the bytes across the link per step are the lines and indices up, and the
+        # drawn pixels read and written in place (counted from a draw into zeros)
+        ref = torch.zeros(ls.shape, dtype=torch.float32, device=dev)
+        draw_lines(ref, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
+        drawn = int((ref != 0).sum())
+        del ref
         e2e = {'value': world * N / (e_ms * 1e-3) / 1e6, 'unit': 'Mlines/s',
                'ms_per_step': e_ms,
-               'h2d_bytes_per_step': int(h_out.numel() * 4 + h_lines.numel() * 4 + h_idxs.numel() * 4),
-               'd2h_bytes_per_step': int(h_out.numel() * 4)}
+               'h2d_bytes_per_step': int(h_lines.numel() * 4 + h_idxs.numel() * 4 + drawn * 4),
+               'd2h_bytes_per_step': int(drawn * 4),
+               'frames': 'page-locked host memory, drawn pixels combined in place by the '
+                         'kernels (zero-copy); %d of %d pixels drawn' % (drawn, h_out.numel())}
 
     if rank != 0:
         if dist is not None:

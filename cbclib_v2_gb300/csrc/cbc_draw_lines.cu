@@ -813,9 +813,149 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
     return CBC_OK;
 }
 
+/* ---- frames in page-locked host memory ------------------------------------------
+ * The lines are drawn into a device scratch that holds the overlap's identity (max:
+ * -inf, which every contribution exceeds; sum: -0, which no contribution leaves
+ * behind), so afterwards a scratch pixel differs from the identity exactly where
+ * some line drew.  One pass then combines those pixels into the host frames through
+ * their device mapping (NVLink-C2C on GB300: coherent loads and stores from the SMs)
+ * and puts the identity back, so the scratch is ready for the next call; the pixels
+ * no line drew never cross the link.  max: host = std::max(host, max of the lines'
+ * values), which is the sequential result (max is exact); sum: host + (sum of the
+ * lines' values), the sum in another order. */
+template <typename T> struct IdentityBits;
+template <> struct IdentityBits<float> {
+    using U = unsigned;
+    static __host__ __device__ U max_bits() { return 0xff800000u; }   /* -inf */
+    static __host__ __device__ U sum_bits() { return 0x80000000u; }   /* -0   */
+};
+template <> struct IdentityBits<double> {
+    using U = unsigned long long;
+    static __host__ __device__ U max_bits() { return 0xfff0000000000000ull; }
+    static __host__ __device__ U sum_bits() { return 0x8000000000000000ull; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+fill_identity_kernel(T *__restrict__ p, long long n, typename IdentityBits<T>::U bits)
+{
+    using U = typename IdentityBits<T>::U;
+    U *q = reinterpret_cast<U *>(p);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        q[i] = bits;
+}
+
+template <typename T, int OV>
+__global__ void __launch_bounds__(kThreads)
+combine_host_kernel(T *__restrict__ host, T *__restrict__ scratch, long long n,
+                    const DevStatus *st)
+{
+    using U = typename IdentityBits<T>::U;
+    if (st->flags & kFatal) return;          /* nothing was drawn */
+    const U id = OV == CBC_MAX ? IdentityBits<T>::max_bits() : IdentityBits<T>::sum_bits();
+    U *sb = reinterpret_cast<U *>(scratch);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const U b = sb[i];
+        if (b != id) {
+            T d;
+            memcpy(&d, &b, sizeof d);
+            const T h = host[i];
+            host[i] = OV == CBC_MAX ? (h < d ? d : h) : h + d;
+            sb[i] = id;
+        }
+    }
+}
+
+template <typename T>
+int draw_lines_host_impl(T *host_out, long long n_frames, long long H, long long W,
+                         const T *lines, long long n_lines, const void *idxs, int idx_bytes,
+                         T max_val, int kernel, int overlap, T *scratch, int fill,
+                         void *workspace, size_t ws_bytes, long long capacity,
+                         long long ck_capacity, const cbc_tuning *tuning, void *stream)
+{
+    g_error.clear();
+    const long long n = n_frames * H * W;
+    if (n_frames < 0 || H < 0 || W < 0) return fail(CBC_ERR_INVALID, "negative size");
+    if (overlap != CBC_SUM && overlap != CBC_MAX)
+        return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if (n > 0 && (!host_out || !scratch)) return fail(CBC_ERR_INVALID, "null pointer");
+    T *dev_host = nullptr;
+    if (n > 0) {
+        /* the device address of the host frames: page-locked memory only */
+        cudaError_t e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&dev_host),
+                                                 host_out, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CBC_ERR_INVALID, "out is not page-locked host memory the device can "
+                                         "address (" + std::string(cudaGetErrorString(e)) + ")");
+        }
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long most = (long long)(sms > 0 ? sms : 132) * 16;
+    long long blocks = (n + kThreads - 1) / kThreads;
+    if (blocks > most) blocks = most;
+    using U = typename IdentityBits<T>::U;
+    const U id = overlap == CBC_MAX ? IdentityBits<T>::max_bits() : IdentityBits<T>::sum_bits();
+    if (fill && n > 0) {
+        fill_identity_kernel<T><<<(unsigned)blocks, kThreads, 0, s>>>(scratch, n, id);
+        note_launches(1);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    int rc = draw_lines_impl<T>(scratch, n_frames, H, W, lines, n_lines, idxs, idx_bytes, max_val,
+                                kernel, overlap, workspace, ws_bytes, capacity, ck_capacity,
+                                tuning, stream);
+    if (rc != CBC_OK) return rc;
+    if (n > 0) {
+        const DevStatus *st = reinterpret_cast<const DevStatus *>(workspace);
+        if (overlap == CBC_MAX)
+            combine_host_kernel<T, CBC_MAX><<<(unsigned)blocks, kThreads, 0, s>>>(dev_host, scratch,
+                                                                                n, st);
+        else
+            combine_host_kernel<T, CBC_SUM><<<(unsigned)blocks, kThreads, 0, s>>>(dev_host, scratch,
+                                                                                n, st);
+        note_launches(1);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return CBC_OK;
+}
+
 }  // namespace cbc
 
 extern "C" {
+
+int cbc_draw_lines_host_f32(float *host_out, int64_t n_frames, int64_t height, int64_t width,
+                            const float *lines, int64_t n_lines, const void *idxs,
+                            int32_t idx_bytes, float max_val, int32_t kernel, int32_t overlap,
+                            float *scratch, int32_t fill, void *workspace,
+                            size_t workspace_bytes, int64_t pair_capacity,
+                            int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
+{
+    return cbc::draw_lines_host_impl<float>(host_out, n_frames, height, width, lines, n_lines,
+                                            idxs, idx_bytes, max_val, kernel, overlap, scratch,
+                                            fill, workspace, workspace_bytes, pair_capacity,
+                                            checkpoint_capacity, tuning, stream);
+}
+
+int cbc_draw_lines_host_f64(double *host_out, int64_t n_frames, int64_t height, int64_t width,
+                            const double *lines, int64_t n_lines, const void *idxs,
+                            int32_t idx_bytes, double max_val, int32_t kernel, int32_t overlap,
+                            double *scratch, int32_t fill, void *workspace,
+                            size_t workspace_bytes, int64_t pair_capacity,
+                            int64_t checkpoint_capacity, const cbc_tuning *tuning, void *stream)
+{
+    return cbc::draw_lines_host_impl<double>(host_out, n_frames, height, width, lines, n_lines,
+                                             idxs, idx_bytes, max_val, kernel, overlap, scratch,
+                                             fill, workspace, workspace_bytes, pair_capacity,
+                                             checkpoint_capacity, tuning, stream);
+}
+
 
 size_t cbc_draw_lines_workspace_size(int64_t n_frames, int64_t height, int64_t width,
                                      int64_t n_lines, int64_t pair_capacity,

@@ -461,183 +461,60 @@ def draw_lines(out, lines, idxs=None, max_val: float = 1.0, kernel: str = 'recta
                       lambda dev_out: _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov))
 
 
-_STAGE_CHUNKS = 16
-_STAGE_CHUNK_BYTES = 290e6
-
-
-class _Stager:
-    """Pipelined staging of page-locked host frames for one (device, host thread): the
-    frames go up, are drawn and come back in chunks of frames on three streams, so
-    that the copies in both directions and the kernels overlap."""
-
-    def __init__(self, dev: torch.device):
-        self.device = dev
-        self.s_in = torch.cuda.Stream(dev)
-        self.s_draw = torch.cuda.Stream(dev)
-        self.s_out = torch.cuda.Stream(dev)
-        self.status_bytes = int(_native.lib().cbc_status_bytes())
-        self.status = torch.zeros((_STAGE_CHUNKS, self.status_bytes),
-                                  dtype=torch.uint8).pin_memory()
-        self.buffer: Optional[torch.Tensor] = None
-        self.ck_per_line = 16.0          # walk checkpoints reserved per line (learned)
-
-    def workspace(self, nbytes: int) -> torch.Tensor:
-        if self.buffer is None or self.buffer.numel() < nbytes:
-            self.buffer = torch.empty(int(nbytes * 1.1) + 4096, dtype=torch.uint8,
-                                      device=self.device)
-        return self.buffer
-
-
-_stagers: dict = {}
-
-
-def _stager(dev: torch.device) -> _Stager:
-    key = (dev.index, threading.get_ident())
-    st = _stagers.get(key)
-    if st is None:
-        with _ws_lock:
-            st = _stagers.setdefault(key, _Stager(dev))
-    return st
-
-
-def _stage_chunks(F: int, frame_bytes: int) -> int:
-    """chunks of about 290 MB overlap the two copy directions best on GB300 (measured
-    on 1.15 GB stacks: 7.96 ms up and down in 4 chunks, 8.3 ms in 8, 9.1 ms in 2)"""
-    return max(2, min(F, _STAGE_CHUNKS, round(F * frame_bytes / _STAGE_CHUNK_BYTES)))
+_host_scratch: dict = {}
 
 
 def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: int,
                        overlap: int) -> bool:
-    """draw_lines on page-locked host frames of 2-D lines, pipelined by chunks of
-    frames.  The upward copies start first (they leave the caller's frames alone);
-    every check that can fail happens before the first frame comes back: frame indices
-    (IndexError, frames untouched, as the synchronous path) and a bound on the
-    coordinates under which no walk can exceed the walk limit (otherwise False: the
-    caller takes the synchronous path, which reports such lines).  A chunk whose walk
-    checkpoints did not fit draws nothing and is drawn again synchronously.  Returns
-    False when the frames do not qualify (pageable, non-contiguous, fewer than 4
-    frames, 3-D lines or no device)."""
+    """draw_lines on page-locked host frames of 2-D lines without copying the frames:
+    the kernels draw into a device scratch holding the overlap's identity and combine
+    the drawn pixels into the host frames through their device mapping
+    (cbc_draw_lines_host_*).  The scratch (one per device, stream and host thread) is
+    left at the identity after every call; it is filled again only when the overlap,
+    the dtype or the size changes.  Returns False when the frames do not qualify
+    (pageable, non-contiguous, 3-D lines or no device)."""
     if not (host.is_pinned() and host.is_contiguous() and host.dim() >= 2 and
             host.dtype in (torch.float32, torch.float64)):
         return False
-    F, H, W = _frames_of(host)
-    if F < 4 or H * W == 0 or _device.get_device() != 'cuda':
+    if _device.get_device() != 'cuda':
         return False
     t = torch.as_tensor(lines)
     if t.ndim < 1 or t.shape[-1] != 5:
         return False
+    F, H, W = _frames_of(host)
     dev = torch.device('cuda', torch.cuda.current_device())
     ln = _as_device_lines(t, dev, host.dtype)
     n = ln.shape[0]
     ix = _as_device_idxs(idxs, n, dev)
-    if ix is None and n != F:
+    if ix is None and n and F != 1 and F != n:
         raise ValueError(f"idxs has an incompatible size ({n} != {F})")
     elem = 4 if host.dtype == torch.float32 else 8
-    frame_bytes = H * W * elem
-    nch = _stage_chunks(F, frame_bytes)
-    bounds = [F * j // nch for j in range(nch + 1)]
-    st = _stager(dev)
-    cur = torch.cuda.current_stream(dev)
-    dev_out = torch.empty(host.shape, dtype=host.dtype, device=dev)
-    st.s_in.wait_stream(cur)
-    ev_in = []
-    for j in range(nch):
-        with torch.cuda.stream(st.s_in):
-            dev_out[bounds[j]:bounds[j + 1]].copy_(host[bounds[j]:bounds[j + 1]],
-                                                   non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record(st.s_in)
-        ev_in.append(ev)
-    try:
-        if ix is None:
-            ix = torch.arange(n, device=dev)
-        bnd = torch.tensor(bounds, device=dev, dtype=torch.int64)
-        srt, order = torch.sort(ix.to(torch.int64), stable=True)
-        pos = torch.searchsorted(srt, bnd)
-        lim = 2.0 ** 20        # |coordinate|, width < 2^20: every walk is below 2^22 px
-        ok = torch.where(torch.isfinite(ln), ln.abs() < lim, True).all()
-        if n:
-            info = torch.cat([srt[:1], srt[-1:], pos, ok.to(torch.int64).reshape(1)]).cpu()
-            lo, hi = int(info[0]), int(info[1])
-            if lo < 0 or hi >= F:
-                raise IndexError(f"idxs range ({lo}, {hi}) is outside of (0, {F})")
-            if not int(info[-1]):
-                st.s_in.synchronize()
-                return False
-            pos = [int(v) for v in info[2:3 + nch]]
-        else:
-            pos = [0] * (nch + 1)
-    except BaseException:
-        st.s_in.synchronize()            # dev_out is still being written
-        raise
-    chunk = torch.bucketize(srt, bnd, right=True) - 1
-    idx_rb = (srt - bnd[chunk.clamp_(0, nch - 1)]).to(torch.int32)
-    lines_s = ln[order].contiguous()
     lib = _native.lib()
-    fn = lib.cbc_draw_lines_f32 if elem == 4 else lib.cbc_draw_lines_f64
-    sizes, caps = [], []
-    for j in range(nch):
-        nj = pos[j + 1] - pos[j]
-        cap, ck = 4 * nj + 1024, int(st.ck_per_line * nj) + 1024
-        nb = lib.cbc_draw_lines_workspace_size(bounds[j + 1] - bounds[j], H, W, nj, cap, ck,
-                                               elem, None)
-        sizes.append((nb + 255) // 256 * 256)
-        caps.append((cap, ck))
-    if st.status.shape[0] < nch:
-        st.status = torch.zeros((nch, st.status_bytes), dtype=torch.uint8).pin_memory()
-    buf = st.workspace(sum(sizes))
-    base = buf.data_ptr()
-    offs = [0]
-    for nb in sizes:
-        offs.append(offs[-1] + nb)
-    st.s_draw.wait_stream(cur)
-    sdraw = st.s_draw.cuda_stream
-    failed = []
-    try:
-        for j in range(nch):
-            f0, f1 = bounds[j], bounds[j + 1]
-            l0, l1 = pos[j], pos[j + 1]
-            st.s_draw.wait_event(ev_in[j])
-            if l1 > l0:
-                rc = fn(dev_out.data_ptr() + f0 * frame_bytes, f1 - f0, H, W,
-                        lines_s.data_ptr() + l0 * 5 * elem, l1 - l0,
-                        idx_rb.data_ptr() + 4 * l0, 4, max_val, kernel, overlap,
-                        base + offs[j], sizes[j], caps[j][0], caps[j][1], None, sdraw)
-                if rc:
-                    failed.append(rc)
-                    break
-                if lib.cbc_copy_status_async(base + offs[j], st.status[j].data_ptr(), sdraw):
-                    failed.append(_native.CBC_ERR_CUDA)
-                    break
-            ev_d = torch.cuda.Event()
-            ev_d.record(st.s_draw)
-            st.s_out.wait_event(ev_d)
-            with torch.cuda.stream(st.s_out):
-                host[f0:f1].copy_(dev_out[f0:f1], non_blocking=True)
-    finally:
-        st.s_in.synchronize()
-        st.s_draw.synchronize()
-        st.s_out.synchronize()
-        cur.wait_stream(st.s_out)
-    if failed:
-        _raise_rc(failed[0])
-    need = st.ck_per_line
-    for j in range(nch):
-        l0, l1 = pos[j], pos[j + 1]
-        if l1 == l0:
-            continue
-        s = _native.Status()
-        lib.cbc_decode_status(st.status[j].data_ptr(), s)
-        need = max(need, 1.25 * s.checkpoints_needed / (l1 - l0))
-        if s.has(_native.CBC_ERR_CAPACITY):
-            # nothing of this chunk was drawn: draw it with the retrying path
-            f0, f1 = bounds[j], bounds[j + 1]
-            _draw_lines_cuda(dev_out[f0:f1], lines_s[l0:l1], idx_rb[l0:l1], max_val, kernel,
-                             overlap)
-            host[f0:f1].copy_(dev_out[f0:f1])
-        else:
-            _raise_status(s, bounds[j + 1] - bounds[j])
-    st.ck_per_line = need
+    fn = lib.cbc_draw_lines_host_f32 if elem == 4 else lib.cbc_draw_lines_host_f64
+    tuning = getattr(_tls, 'tuning', None)
+    with _on_current_device(dev):
+        stream = _current_stream(dev)
+        key = (dev.index, stream, threading.get_ident())
+        entry = _host_scratch.get(key)
+        tag = (overlap, host.dtype)
+        if entry is None or entry[0].numel() < F * H * W or entry[0].dtype != host.dtype:
+            entry = [torch.empty(F * H * W, dtype=host.dtype, device=dev), None]
+            _host_scratch[key] = entry
+        scratch = entry[0]
+        state = {'fill': int(entry[1] != tag)}
+
+        def call(buf, capacity, ck_capacity, tref, stream):
+            rc = fn(host.data_ptr(), F, H, W, ln.data_ptr(), n,
+                    None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+                    max_val, kernel, overlap, scratch.data_ptr(), state['fill'], buf.data_ptr(),
+                    buf.numel(), capacity, ck_capacity, tref, stream)
+            if rc == 0:
+                state['fill'] = 0      # the scratch is at the identity from here on
+                entry[1] = tag
+            return rc
+
+        entry[1] = None                # unknown until the call has run
+        _run_with_workspace(call, dev, F, H, W, n, elem, tuning)
     return True
 
 

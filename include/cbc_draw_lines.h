@@ -291,6 +291,32 @@ CBC_API int cbc_squared_loss_step_f32(const float *target, int64_t n_frames, int
                                       size_t workspace_bytes, int64_t pair_capacity,
                                       int64_t checkpoint_capacity, void *stream);
 
+/* draw_lines into frames in page-locked host memory (cudaHostAlloc, or registered),
+ * which the kernels address directly (NVLink-C2C on GB300): the lines are drawn into
+ * `scratch` (n_frames * height * width device elements), which must hold the
+ * overlap's identity on entry (-inf for CBC_MAX, -0.0 for CBC_SUM) unless `fill` is 1
+ * (the call writes it first); then the pixels some line drew are combined into
+ * host_out and `scratch` gets the identity back.  Only drawn pixels cross the link.
+ * lines and idxs are device arrays; other arguments, the workspace and the errors as
+ * cbc_draw_lines_f32 (an error leaves host_out untouched).  Pageable host memory is
+ * rejected with CBC_ERR_INVALID.  Replaces the host-array path of the reference's
+ * draw_lines (_src/functions.py:275-302, bresenham.cpp:313-331).  */
+CBC_API int cbc_draw_lines_host_f32(float *host_out, int64_t n_frames, int64_t height,
+                                    int64_t width, const float *lines, int64_t n_lines,
+                                    const void *idxs, int32_t idx_bytes, float max_val,
+                                    int32_t kernel, int32_t overlap, float *scratch,
+                                    int32_t fill, void *workspace, size_t workspace_bytes,
+                                    int64_t pair_capacity, int64_t checkpoint_capacity,
+                                    const cbc_tuning *tuning, void *stream);
+
+CBC_API int cbc_draw_lines_host_f64(double *host_out, int64_t n_frames, int64_t height,
+                                    int64_t width, const double *lines, int64_t n_lines,
+                                    const void *idxs, int32_t idx_bytes, double max_val,
+                                    int32_t kernel, int32_t overlap, double *scratch,
+                                    int32_t fill, void *workspace, size_t workspace_bytes,
+                                    int64_t pair_capacity, int64_t checkpoint_capacity,
+                                    const cbc_tuning *tuning, void *stream);
+
 /* One Adam step on the (N, 5) float32 line parameters of a streak fit, in one kernel:
  * exp_avg = exp_avg + (1 - beta1)(grad - exp_avg),
  * exp_avg_sq = beta2 exp_avg_sq + (1 - beta2) grad^2,
