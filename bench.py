@@ -53,13 +53,18 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--workload', default='detector_stack',
-                   choices=['detector_stack', 'fit', 'ragged', 'fit_loop'],
+                   choices=['detector_stack', 'fit', 'ragged', 'fit_loop', 'rotomap',
+                            'accumulate2d', 'f64'],
                    help='detector_stack: the headline forward; fit: forward + adjoint '
                         'iterations on 8 x 1024^2 frames vs a finite-difference gradient; '
                         'ragged: 256 x 1024^2 frames with lognormal line counts, one '
                         'CUDA-graph launch vs per-frame plain launches; fit_loop: 100 '
                         'Adam steps of the streak fit on 32 x 2167x2070 frames, 160k '
-                        'biweight lines, max overlap')
+                        'biweight lines, max overlap; rotomap: 3-D accumulate_lines as '
+                        'the indexer calls it (4 x 96^3 volumes, 16k lines, max in a '
+                        'streak, sum over streaks); accumulate2d: 2-D accumulate_lines '
+                        'with mixed overlaps (16 x 1024^2, 64k lines); f64: the detector '
+                        'stack in float64')
     args = p.parse_args()
     args.steps_given = any(a == '--steps' or a.startswith('--steps=') for a in sys.argv[1:])
     args.frames_given = any(a == '--frames' or a.startswith('--frames=') for a in sys.argv[1:])
@@ -353,6 +358,129 @@ def run_ragged(args, world, rank, local):
             'graph_speedup_vs_per_frame': ms_frames / ms_graph}), flush=True)
 
 
+def _device_steps(fn, args, local):
+    """W untimed calls, then K calls between CUDA events on the current stream, with
+    the clocks sampled in between; returns (ms per call, clocks)"""
+    import torch
+    for _ in range(max(args.warmup, 1)):
+        fn()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
+    a.record(stream)
+    for _ in range(args.steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    clocks.end()
+    return a.elapsed_time(b) / args.steps, clocks.stop()
+
+
+def run_accumulate(args, world, rank, local):
+    """accumulate_lines throughput (device-resident), next to the oracle's CPU
+    accumulate_lines (one thread: the reference's accumulate_lines loops over terms
+    serially, bresenham.cpp:151-259) on the first frames"""
+    import torch
+    import oracle
+    from cbclib_v2_gb300 import _native, accumulate_lines, workloads
+    torch.cuda.set_device(local)
+    ts = (workloads.rotomap_stack(seed=5000 + rank) if args.workload == 'rotomap'
+          else workloads.accumulate_stack(seed=5100 + rank))
+    dev = torch.device('cuda', local)
+    lines = torch.from_numpy(ts.lines.astype(np.float32)).to(dev)
+    terms = torch.from_numpy(ts.terms.astype(np.int32)).to(dev)
+    frames = torch.from_numpy(ts.frames.astype(np.int32)).to(dev)
+    out = torch.zeros(ts.shape, dtype=torch.float32, device=dev)
+
+    def step():
+        accumulate_lines(out, lines, terms, frames, ts.max_val, ts.kernel, ts.in_overlap,
+                         ts.out_overlap)
+
+    _native.profile_enable(True)
+    _native.profile_read(reset=True)
+    ms, clocks = _device_steps(step, args, local)
+    prof = _native.profile_read(reset=True)
+    _native.profile_enable(False)
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        k = 1
+        sub = ts.subset(k)
+        while True:
+            o = np.zeros(sub.shape, np.float32)
+            t0 = time.perf_counter()
+            oracle.accumulate_lines(o, sub.lines.astype(np.float32), sub.terms, sub.frames,
+                                    sub.max_val, sub.kernel, sub.in_overlap, sub.out_overlap)
+            sec = time.perf_counter() - t0
+            if sec > 5.0 or k >= ts.shape[0]:
+                break
+            k = min(ts.shape[0], k * 2)
+            sub = ts.subset(k)
+        cb = {'value': sub.n_lines / sec / 1e6, 'unit': 'Mlines/s', 'cores': 1, 'kind': 'port',
+              'sample': f'{k} of {ts.shape[0]} frames ({sub.n_lines} lines), one run'}
+    if rank == 0:
+        print(json.dumps({
+            'metric': 'accumulate_lines throughput', 'value': world * ts.n_lines / ms / 1e3,
+            'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': ts.name, 'shape': list(ts.shape), 'lines': ts.n_lines,
+                       'terms': int(ts.frames.size), 'kernel': ts.kernel,
+                       'in_overlap': ts.in_overlap, 'out_overlap': ts.out_overlap,
+                       'out': 'accumulated in place, not re-zeroed between steps'},
+            'clocks': clocks, 'gpu_launches': prof.launches, 'cpu_baseline': cb}), flush=True)
+
+
+def run_f64(args, world, rank, local):
+    """the detector stack drawn in float64 (lines and frames), device-resident, next to
+    the oracle's float64 draw_lines on all host threads"""
+    import torch
+    import oracle
+    from cbclib_v2_gb300 import _native, draw_lines, workloads
+    torch.cuda.set_device(local)
+    ls = workloads.detector_stack(seed=1000 + rank, F=args.frames)
+    dev = torch.device('cuda', local)
+    lines = torch.from_numpy(ls.lines.astype(np.float64)).to(dev)
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)
+    out = torch.zeros(ls.shape, dtype=torch.float64, device=dev)
+    _native.profile_enable(True)
+    _native.profile_read(reset=True)
+    ms, clocks = _device_steps(
+        lambda: draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap), args, local)
+    prof = _native.profile_read(reset=True)
+    _native.profile_enable(False)
+    F, H, W = ls.shape
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sub = workloads.frames_subset(ls, [0, 1])
+        o = np.zeros(sub.shape, np.float64)
+        threads = len(os.sched_getaffinity(0))
+        t0 = time.perf_counter()
+        oracle.draw_lines(o, sub.lines, sub.idxs, sub.max_val, sub.kernel, sub.overlap, threads)
+        sec = time.perf_counter() - t0
+        cb = {'value': sub.n_lines / sec / 1e6, 'unit': 'Mlines/s', 'cores': threads,
+              'kind': 'port', 'sample': f'2 of {F} frames ({sub.n_lines} lines), one run'}
+    render_ms = prof.ms_render / max(prof.calls, 1)
+    contract = 2 * F * H * W * 8 + 44 * ls.n_lines
+    peak, src = measured_peak()
+    if rank == 0:
+        print(json.dumps({
+            'metric': 'draw_lines throughput', 'value': world * ls.n_lines / ms / 1e3,
+            'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': ls.name + '_f64', 'frames': F, 'lines': ls.n_lines,
+                       'kernel': ls.kernel, 'overlap': ls.overlap, 'out_dtype': 'float64'},
+            'roofline': {'bound': 'hbm', 'achieved': contract / (render_ms * 1e-3) / 1e9,
+                         'peak': peak, 'peak_source': src, 'unit': 'GB/s',
+                         'frac': contract / (render_ms * 1e-3) / 1e9 / peak, 'traffic': None,
+                         'bytes_model': '2*F*H*W*8 + 44*N over the render kernel time',
+                         'kernel': 'segments_kernel', 'ms_per_launch': render_ms},
+            'clocks': clocks, 'gpu_launches': prof.launches, 'cpu_baseline': cb}), flush=True)
+
+
 def run_fit_loop(args, world, rank, local):
     """the streak-fit loop: 32 frames of 2167x2070, 5,000 biweight lines per frame,
     max overlap; the target is Poisson noise on the render of the true lines (peak 100
@@ -405,6 +533,12 @@ def main():
     world, rank, local = dist_env()
     if args.workload == 'fit_loop' and args.impl == 'gb300':
         run_fit_loop(args, world, rank, local)
+        return
+    if args.workload in ('rotomap', 'accumulate2d') and args.impl == 'gb300':
+        run_accumulate(args, world, rank, local)
+        return
+    if args.workload == 'f64' and args.impl == 'gb300':
+        run_f64(args, world, rank, local)
         return
     if args.workload == 'fit' and args.impl == 'gb300':
         run_fit(args, world, rank, local)

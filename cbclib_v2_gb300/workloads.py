@@ -117,3 +117,68 @@ def perturbed(lines: np.ndarray, seed: int, sigma_pt: float = 0.5,
     out[:, :4] += rng.normal(0.0, sigma_pt, (lines.shape[0], 4))
     out[:, 4] = np.maximum(out[:, 4] + rng.normal(0.0, sigma_w, lines.shape[0]), 0.5)
     return out
+
+
+@dataclass
+class TermSet:
+    """accumulate_lines inputs: line i belongs to term terms[i], term t to frame
+    frames[t]; lines are (N, 5) for frames or (N, 7) for volumes"""
+    name: str
+    shape: Tuple[int, ...]           # (frames, height, width) or (frames, depth, height, width)
+    lines: np.ndarray
+    terms: np.ndarray                # (N,) int64
+    frames: np.ndarray               # (T,) int64
+    kernel: str
+    in_overlap: str
+    out_overlap: str
+    max_val: float = 1.0
+
+    @property
+    def n_lines(self) -> int:
+        return int(self.lines.shape[0])
+
+    def subset(self, n_frames: int) -> 'TermSet':
+        """the terms (and their lines) of the first n_frames frames"""
+        keep_t = np.flatnonzero(self.frames < n_frames)
+        remap = -np.ones(self.frames.size, np.int64)
+        remap[keep_t] = np.arange(keep_t.size)
+        keep_l = np.flatnonzero(np.isin(self.terms, keep_t))
+        return TermSet(self.name, (n_frames,) + tuple(self.shape[1:]), self.lines[keep_l],
+                       remap[self.terms[keep_l]], self.frames[keep_t], self.kernel,
+                       self.in_overlap, self.out_overlap, self.max_val)
+
+
+def rotomap_stack(seed: int = 0, F: int = 4, D: int = 96, streaks: int = 500,
+                  per_streak: int = 8) -> TermSet:
+    """accumulate_lines as the indexer's rotomap calls it: F rotation-space volumes of
+    D^3 voxels; each volume has `streaks` terms (streaks) of `per_streak` 3-D
+    segments (candidate tilt lines: uniform start, isotropic direction, length
+    U(10, 60) voxels, width 2), combined with max within a streak and summed over the
+    streaks; gaussian profile."""
+    rng = np.random.default_rng(seed)
+    n_terms = F * streaks
+    n = n_terms * per_streak
+    p0 = rng.random((n, 3)) * D
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    p1 = p0 + v * rng.uniform(10, 60, n)[:, None]
+    lines = np.concatenate([p0, p1, np.full((n, 1), 2.0)], axis=1)
+    terms = np.repeat(np.arange(n_terms, dtype=np.int64), per_streak)
+    frames = np.repeat(np.arange(F, dtype=np.int64), streaks)
+    return TermSet(f'rotomap_{F}x{D}^3', (F, D, D, D), lines, terms, frames, 'gaussian',
+                   'max', 'sum')
+
+
+def accumulate_stack(seed: int = 0, F: int = 16, H: int = 1024, W: int = 1024,
+                     terms_per_frame: int = 1000, per_term: int = 4) -> TermSet:
+    """2-D accumulate_lines with mixed overlaps: F frames of H x W, terms of
+    `per_term` segments of the single-frame distribution (length U(10, 100), width
+    U(1, 5)) summed within a term, the terms combined with max; triangular profile."""
+    rng = np.random.default_rng(seed)
+    n_terms = F * terms_per_frame
+    n = n_terms * per_term
+    lines = _segments(rng, n, H, W, rng.uniform(10, 100, n), rng.uniform(1, 5, n))
+    terms = np.repeat(np.arange(n_terms, dtype=np.int64), per_term)
+    frames = np.repeat(np.arange(F, dtype=np.int64), terms_per_frame)
+    return TermSet(f'accumulate_{F}x{H}x{W}', (F, H, W), lines, terms, frames, 'triangular',
+                   'sum', 'max')
