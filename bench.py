@@ -381,8 +381,8 @@ def _device_steps(fn, args, local):
 
 def run_accumulate(args, world, rank, local):
     """accumulate_lines throughput (device-resident), next to the oracle's CPU
-    accumulate_lines (one thread: the reference's accumulate_lines loops over terms
-    serially, bresenham.cpp:151-259) on the first frames"""
+    accumulate_lines (terms shared out among all host threads, as the reference does,
+    bresenham.cpp:151-259) on the first frames"""
     import torch
     import oracle
     from cbclib_v2_gb300 import _native, accumulate_lines, workloads
@@ -406,19 +406,22 @@ def run_accumulate(args, world, rank, local):
     _native.profile_enable(False)
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
+        threads = len(os.sched_getaffinity(0))
         k = 1
         sub = ts.subset(k)
         while True:
             o = np.zeros(sub.shape, np.float32)
             t0 = time.perf_counter()
             oracle.accumulate_lines(o, sub.lines.astype(np.float32), sub.terms, sub.frames,
-                                    sub.max_val, sub.kernel, sub.in_overlap, sub.out_overlap)
+                                    sub.max_val, sub.kernel, sub.in_overlap, sub.out_overlap,
+                                    threads)
             sec = time.perf_counter() - t0
             if sec > 5.0 or k >= ts.shape[0]:
                 break
             k = min(ts.shape[0], k * 2)
             sub = ts.subset(k)
-        cb = {'value': sub.n_lines / sec / 1e6, 'unit': 'Mlines/s', 'cores': 1, 'kind': 'port',
+        cb = {'value': sub.n_lines / sec / 1e6, 'unit': 'Mlines/s', 'cores': threads,
+              'kind': 'port',
               'sample': f'{k} of {ts.shape[0]} frames ({sub.n_lines} lines), one run'}
     if rank == 0:
         print(json.dumps({

@@ -39,7 +39,7 @@ def _load():
             f.restype = ctypes.c_int
             f = getattr(lib, f'cbc_oracle_accumulate_lines_{sfx}')
             f.argtypes = [p, i64, ctypes.c_int, p, p, i64, p, p, i64, real, ctypes.c_int,
-                          ctypes.c_int, ctypes.c_int]
+                          ctypes.c_int, ctypes.c_int, ctypes.c_int]
             f.restype = ctypes.c_int
             f = getattr(lib, f'cbc_oracle_profile_{sfx}')
             f.argtypes = [ctypes.c_int, real]
@@ -104,8 +104,9 @@ def draw_lines(out: np.ndarray, lines: np.ndarray, idxs: Optional[np.ndarray] = 
 
 def accumulate_lines(out: np.ndarray, lines: np.ndarray, terms: np.ndarray, frames: np.ndarray,
                      max_val: float = 1.0, kernel: str = 'rectangular', in_overlap: str = 'sum',
-                     out_overlap: str = 'sum') -> np.ndarray:
-    """Reference-semantics ``accumulate_lines`` on the CPU (mutates and returns ``out``)."""
+                     out_overlap: str = 'sum', num_threads: int = 1) -> np.ndarray:
+    """Reference-semantics ``accumulate_lines`` on the CPU (mutates and returns ``out``),
+    terms shared out among ``num_threads`` threads as the reference does."""
     lib = _load()
     if out.dtype not in (np.float32, np.float64) or not out.flags.c_contiguous:
         raise ValueError("out must be a C-contiguous float32/float64 array")
@@ -125,7 +126,8 @@ def accumulate_lines(out: np.ndarray, lines: np.ndarray, terms: np.ndarray, fram
                          f"{out_overlap}")
     rc = getattr(lib, f'cbc_oracle_accumulate_lines_{sfx}')(
         _ptr(out), n_frames, ndim, _ptr(shape), _ptr(ln), ln.shape[0], _ptr(tm), _ptr(fr),
-        fr.size, max_val, KERNELS[kernel], OVERLAPS[in_overlap], OVERLAPS[out_overlap])
+        fr.size, max_val, KERNELS[kernel], OVERLAPS[in_overlap], OVERLAPS[out_overlap],
+        int(num_threads))
     _raise(rc, 'accumulate_lines')
     return out
 

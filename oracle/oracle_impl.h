@@ -441,11 +441,14 @@ static int OF(oterm_cmp)(const void *a, const void *b)
 
 /* accumulate_lines_nd_impl (bresenham.cpp:151-259): lines grouped by term (stable in
  * line order), each term rendered into a scratch frame with in_overlap, then combined
- * into frame frames[term] of `out` with out_overlap.  Terms run in ascending order. */
+ * into frame frames[term] of `out` with out_overlap.  Like the reference, the terms are
+ * shared out among num_threads threads (bresenham.cpp:200-206), each with its own
+ * scratch frame; a term's merge into `out` runs in a critical section.  With one
+ * thread the terms run in ascending order. */
 int OF(cbc_oracle_accumulate_lines)(OT *out, int64_t n_frames, int ndim, const int64_t *shape,
                                     const OT *lines, int64_t n_lines, const int64_t *terms,
                                     const int64_t *frames, int64_t n_terms, OT max_val,
-                                    int kernel, int in_overlap, int out_overlap)
+                                    int kernel, int in_overlap, int out_overlap, int num_threads)
 {
     if (ndim != 2 && ndim != 3) return 1;
     if (kernel < 0 || kernel > 4) return 1;
@@ -457,32 +460,44 @@ int OF(cbc_oracle_accumulate_lines)(OT *out, int64_t n_frames, int ndim, const i
     for (int64_t i = 0; i < n_lines; i++) if (terms[i] < 0 || terms[i] >= n_terms) return 2;
     int64_t *order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n_lines ? n_lines : 1));
     int64_t *offs = (int64_t *)calloc((size_t)n_terms + 1, sizeof(int64_t));
-    OF(oacc_ctx) c = {NULL, NULL, 0, 0, 0, max_val, kernel, in_overlap};
-    c.scratch = (OT *)calloc((size_t)(fsize ? fsize : 1), sizeof(OT));
-    if (!order || !offs || !c.scratch) { free(order); free(offs); free(c.scratch); return 1; }
+    if (!order || !offs) { free(order); free(offs); return 1; }
     for (int64_t i = 0; i < n_lines; i++) order[i] = i;
     OF(osort_terms_keys) = (int64_t *)terms;
     qsort(order, (size_t)n_lines, sizeof(int64_t), OF(oterm_cmp));
     for (int64_t i = 0; i < n_lines; i++) offs[terms[i] + 1]++;
     for (int64_t t = 0; t < n_terms; t++) offs[t + 1] += offs[t];
-    OF(osink) sink = {ndim, shape, (OT)0, OF(oacc_emit), &c};
-    for (int64_t t = 0; t < n_terms; t++) {
-        for (int64_t k = offs[t]; k < offs[t + 1]; k++) {
-            int64_t i = order[k];
-            sink.width = lines[L * i + 2 * ndim];
-            OF(odraw_line)(lines + L * i, ndim, &sink);
+    int rc = 0;
+    if (num_threads < 1) num_threads = 1;
+#pragma omp parallel num_threads(num_threads)
+    {
+        OF(oacc_ctx) c = {NULL, NULL, 0, 0, 0, max_val, kernel, in_overlap};
+        c.scratch = (OT *)calloc((size_t)(fsize ? fsize : 1), sizeof(OT));
+        if (!c.scratch) c.failed = 1;
+        OF(osink) sink = {ndim, shape, (OT)0, OF(oacc_emit), &c};
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t t = 0; t < n_terms; t++) {
+            if (c.failed) continue;
+            for (int64_t k = offs[t]; k < offs[t + 1]; k++) {
+                int64_t i = order[k];
+                sink.width = lines[L * i + 2 * ndim];
+                OF(odraw_line)(lines + L * i, ndim, &sink);
+            }
+            OT *dst = out + frames[t] * fsize;
+#pragma omp critical(oracle_accumulate_merge)
+            for (size_t k = 0; k < c.ntouched; k++) {
+                int64_t f = c.touched[k];
+                if (out_overlap) dst[f] = OF(omax)(dst[f], c.scratch[f]);
+                else dst[f] = c.scratch[f] + dst[f];
+                c.scratch[f] = (OT)0;
+            }
+            c.ntouched = 0;
         }
-        OT *dst = out + frames[t] * fsize;
-        for (size_t k = 0; k < c.ntouched; k++) {
-            int64_t f = c.touched[k];
-            if (out_overlap) dst[f] = OF(omax)(dst[f], c.scratch[f]);
-            else dst[f] = c.scratch[f] + dst[f];
-            c.scratch[f] = (OT)0;
-        }
-        c.ntouched = 0;
+#pragma omp critical(oracle_accumulate_rc)
+        if (c.failed) rc = 1;
+        free(c.scratch);
+        free(c.touched);
     }
-    int rc = c.failed;
-    free(order); free(offs); free(c.scratch); free(c.touched);
+    free(order); free(offs);
     return rc;
 }
 
