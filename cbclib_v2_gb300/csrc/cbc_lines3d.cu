@@ -348,21 +348,15 @@ struct Emit3 {
         case 0:  atomicAdd(out + fbase + vox, v); break;
         case 1:  global_combine_max(out + fbase + vox, v); break;
         case 4 + kAccSumSum: atomicAdd(out + fbase + vox, v); break;
-        case 4 + kAccMaxMax: global_combine_max(out + fbase + vox, T(0) < v ? v : T(0)); break;
-        case 4 + kAccMaxSum:
-            table_combine<T, 1>(keys, vals, mask, term_of_line[line], vox, v, st);
-            break;
-        default:
-            table_combine<T, 0>(keys, vals, mask, term_of_line[line], vox, v, st);
-            break;
+        default:  global_combine_max(out + fbase + vox, T(0) < v ? v : T(0)); break;
         }
     }
 };
 
 /* a visited voxel: the error, and for error <= 1 inside the volume, the emit */
-template <typename T, int K>
+template <typename T, class EM>
 __device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, const Vol &v,
-                                      long long fbase, int line, const Emit3<T, K> &emit)
+                                      long long fbase, int line, const EM &emit)
 {
     const T E = error(r, it);
     if (!(E <= T(1))) return;
@@ -384,9 +378,9 @@ __device__ __forceinline__ It3<T> collapse(const Rec3<T> &r, const It3<T> &src, 
 
 /* one column of draw_line_3d (bresenham.hpp:392-428): the centre voxel and the four
  * quadrants of the short-axis plane */
-template <typename T, int K>
+template <typename T, class EM>
 __device__ void draw_column(const Rec3<T> &r, const It3<T> &it, const Vol &v, long long fbase,
-                            int line, const Emit3<T, K> &emit, DevStatus *st)
+                            int line, const EM &emit, DevStatus *st)
 {
     const int ax = r.axis, ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
     visit(r, it, v, fbase, line, emit);
@@ -462,8 +456,280 @@ render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
     }
 }
 
+/* ---- accumulate with mixed overlaps: terms combined in shared memory ----
+ * A term's lines are combined with in_overlap in a zeroed buffer before the buffer is
+ * merged into its frame (bresenham.cpp:151-259).  Here one CTA takes one term at a
+ * time and builds that buffer as an open-addressing (voxel, value) table in shared
+ * memory: the term's (line, column) items are shared out among the threads, every
+ * visited voxel is combined into its slot (in-term max or sum), and afterwards each
+ * drawn voxel is merged into the volume with one global atomic.  A term with more
+ * voxels than the table takes is done in partitions of its voxels (a hash of the voxel
+ * index modulo P; each pass walks all of the term's columns and keeps the voxels of
+ * one partition): P starts from an estimate, and a partition that fills the table is
+ * split in two and redone, so every voxel is merged exactly once and there is no
+ * capacity to run out of. */
+template <typename T> struct TermTable { static constexpr int kBits = 13; };   /* 64 KB */
+template <> struct TermTable<double> { static constexpr int kBits = 12; };       /* 48 KB */
+constexpr int kTermThreads = 256;
+constexpr int kTermChunk = kTermThreads;      /* lines staged per chunk */
+constexpr int kTermStack = 64;                /* pending partitions per term */
+
+template <typename T>
+struct TermArgs {
+    const Rec3<T> *recs;
+    const Ck3<T> *cks;
+    Vol v;
+    DevStatus *st;
+    T *out;
+    T max_val;
+    const int *tcount, *toff, *tlines, *frame_of_term;
+    const float *test;
+    long long n_terms;
+};
+
+template <typename T>
+constexpr size_t term_smem()
+{
+    return (size_t)(1 << TermTable<T>::kBits) * (sizeof(int) + sizeof(T));
+}
+
+/* after prep3: each drawable line adds itself to its term's count and a typical voxel
+ * count, columns x pi (0.9 w + 0.5)^2, to the term's estimate (only the starting
+ * number of partitions depends on it) */
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+term_count3_kernel(const Rec3<T> *__restrict__ recs, const int *__restrict__ term_of_line,
+                   long long n_lines, int *__restrict__ tcount, float *__restrict__ test)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines || recs[i].ncols <= 0) return;
+    const int t = term_of_line[i];
+    atomicAdd(&tcount[t], 1);
+    const float r = 0.9f * (float)recs[i].w + 0.5f;
+    atomicAdd(&test[t], (float)recs[i].ncols * 3.14159265f * r * r);
+}
+
+/* each term's first slot in the line list: block scan, one cursor atomic per block */
+__global__ void __launch_bounds__(kThreads)
+term_offsets_kernel(const int *__restrict__ tcount, int *__restrict__ toff,
+                    int *__restrict__ tfill, long long n_terms, unsigned long long *cursor)
+{
+    __shared__ int warp_sums[kThreads / 32];
+    __shared__ unsigned long long block_base;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t < n_terms ? tcount[t] : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int v = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        int sum = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, sum, o);
+            if (lane >= o) sum += u;
+        }
+        if (lane < kThreads / 32) warp_sums[lane] = sum - v;
+        if (lane == kThreads / 32 - 1) block_base = atomicAdd(cursor, (unsigned long long)sum);
+    }
+    __syncthreads();
+    if (t >= n_terms) return;
+    const int o = (int)(block_base + (unsigned long long)(warp_sums[wid] + incl - c));
+    toff[t] = o;
+    tfill[t] = o;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+term_fill3_kernel(const Rec3<T> *__restrict__ recs, const int *__restrict__ term_of_line,
+                  long long n_lines, int *__restrict__ tfill, int *__restrict__ tlines)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines || recs[i].ncols <= 0) return;
+    tlines[atomicAdd(&tfill[term_of_line[i]], 1)] = (int)i;
+}
+
+/* the partition of a voxel: hash bits independent of the table slot's */
+__device__ __forceinline__ unsigned voxel_part(int k)
+{
+    unsigned x = (unsigned)k * 0x85ebca6bu;
+    return x ^ (x >> 16);
+}
+
+/* a term's voxels of the current partition into the shared table; `count` grows with
+ * every claimed slot and `full` is raised at 3/4 of the table */
+template <typename T, int K, int IN_MAX>
+struct SmEmit {
+    int *key;
+    T *val;
+    int *count;
+    int *full;
+    T max_val;
+    unsigned pmask, part;
+    __device__ __forceinline__ void operator()(long long, long long vox, int, T E) const {
+        using A = Ar<T>;
+        constexpr int kBits = TermTable<T>::kBits, kSize = 1 << kBits;
+        const int k = (int)vox;
+        if ((voxel_part(k) & pmask) != part) return;
+        if (*reinterpret_cast<volatile int *>(full)) return;    /* this pass is redone */
+        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
+        unsigned h = ((unsigned)k * 2654435761u) >> (32 - kBits);   /* Fibonacci hashing */
+        for (int p = 0; p < kSize; p++) {
+            int cur = *reinterpret_cast<volatile int *>(key + h);
+            if (cur == -1) {
+                cur = atomicCAS(key + h, -1, k);
+                if (cur == -1 && atomicAdd(count, 1) >= kSize * 3 / 4)
+                    *reinterpret_cast<volatile int *>(full) = 1;
+            }
+            if (cur == -1 || cur == k) {
+                if (IN_MAX) term_combine_max(val + h, v);
+                else atomicAdd(val + h, v);
+                return;
+            }
+            h = (h + 1) & (kSize - 1);
+        }
+        *reinterpret_cast<volatile int *>(full) = 1;
+    }
+};
+
+template <typename T, int K, int IN_MAX, int OUT_MAX>
+__global__ void __launch_bounds__(kTermThreads)
+term_render3_kernel(TermArgs<T> a)
+{
+    constexpr int kSize = 1 << TermTable<T>::kBits;
+    extern __shared__ __align__(16) unsigned char term_smem_raw[];
+    T *s_val = reinterpret_cast<T *>(term_smem_raw);
+    int *s_key = reinterpret_cast<int *>(term_smem_raw + sizeof(T) * kSize);
+    __shared__ int s_pre[kTermChunk + 1];
+    __shared__ int s_line[kTermChunk];
+    __shared__ int s_warp[kTermThreads / 32];
+    __shared__ unsigned s_stack[kTermStack];
+    __shared__ int s_depth, s_count, s_full;
+    if (a.st->flags & kFatal) return;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const long long frame_vox = (long long)a.v.D * a.v.H * a.v.W;
+    for (long long t = blockIdx.x; t < a.n_terms; t += gridDim.x) {
+        const int n_t = a.tcount[t];
+        if (n_t == 0) continue;
+        /* pending partitions (part, log2 P), one per 32-bit word */
+        if (tid == 0) {
+            /* at most 32 starting partitions: with one more entry per split, the stack
+             * stays below 32 + 24 entries */
+            const float want = a.test[t] / (0.6f * (float)kSize);
+            int lg = 0;
+            while ((float)(1 << lg) < want && lg < 5) lg++;
+            s_depth = 0;
+            for (int p = (1 << lg) - 1; p >= 0; p--) s_stack[s_depth++] = ((unsigned)p << 5) | lg;
+        }
+        __syncthreads();
+        while (s_depth > 0) {
+            const unsigned top = s_stack[s_depth - 1];
+            const unsigned lg = top & 31u, part = top >> 5;
+            for (int j = tid; j < kSize; j += kTermThreads) {
+                s_key[j] = -1;
+                s_val[j] = T(0);
+            }
+            if (tid == 0) {
+                s_count = 0;
+                s_full = 0;
+            }
+            __syncthreads();
+            const SmEmit<T, K, IN_MAX> emit{s_key, s_val, &s_count, &s_full, a.max_val,
+                                            (1u << lg) - 1u, part};
+            for (int c0 = 0; c0 < n_t && !s_full; c0 += kTermChunk) {
+                /* this chunk's lines and the prefix sum of their columns */
+                const int nc = min(kTermChunk, n_t - c0);
+                int ncol = 0;
+                if (tid < nc) {
+                    const int l = a.tlines[a.toff[t] + c0 + tid];
+                    s_line[tid] = l;
+                    ncol = a.recs[l].ncols;
+                }
+                int incl = ncol;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                if (lane == 31) s_warp[wid] = incl;
+                __syncthreads();
+                int before = 0;
+                for (int w = 0; w < wid; w++) before += s_warp[w];
+                s_pre[tid] = before + incl - ncol;
+                if (tid == kTermThreads - 1) s_pre[kTermThreads] = before + incl;
+                __syncthreads();
+                const int total = s_pre[nc];
+                /* one (line, column) per item: from the column's segment checkpoint, the
+                 * walk to the column, then the column */
+                for (int j = tid; j < total && !*reinterpret_cast<volatile int *>(&s_full);
+                     j += kTermThreads) {
+                    int lo = 0, hi = nc - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s_pre[mid] <= j) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    const int line = s_line[lo], col = j - s_pre[lo];
+                    const Rec3<T> r = a.recs[line];
+                    const Ck3<T> ck = a.cks[r.ck_base + col / kSeg];
+                    if (ck.cur[0] == INT_MIN) continue;
+                    It3<T> it;
+                    for (int i = 0; i < 3; i++) { it.cur[i] = ck.cur[i]; it.step[i] = r.step[i]; }
+                    it.te = ck.te;
+                    for (int i = 0; i < 3; i++) it.ne[i] = ck.ne[i];
+                    update(r, it);
+                    const int ax = r.axis, sa = r.step[ax];
+                    long long guard = 0;
+                    while (!at_end(r, it)) {
+                        if (it.next[ax]) {
+                            const int idx = (it.cur[ax] - r.c0) * sa;
+                            if (idx > col) break;
+                            if (idx == col) {
+                                draw_column(r, it, a.v, 0, line, emit, a.st);
+                                break;
+                            }
+                        }
+                        advance(r, it);
+                        if (++guard > 4LL * CBC_MAX_WALK + 64) {
+                            atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
+                            break;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            if (s_full) {
+                /* too many voxels in this partition: split it, nothing merged */
+                if (tid == 0) {
+                    s_depth--;
+                    if (lg < 24 && s_depth + 2 <= kTermStack) {
+                        s_stack[s_depth++] = ((part + (1u << lg)) << 5) | (lg + 1);
+                        s_stack[s_depth++] = (part << 5) | (lg + 1);
+                    } else {
+                        atomicOr(&a.st->flags, 1 << CBC_ERR_CAPACITY);
+                    }
+                }
+            } else {
+                T *dst = a.out + (long long)a.frame_of_term[t] * frame_vox;
+                for (int j = tid; j < kSize; j += kTermThreads) {
+                    const int k = s_key[j];
+                    if (k < 0) continue;
+                    if (OUT_MAX) global_combine_max(dst + k, s_val[j]);
+                    else atomicAdd(dst + k, s_val[j]);
+                }
+                if (tid == 0) s_depth--;
+            }
+            __syncthreads();
+        }
+    }
+}
+
 struct Layout3 {
-    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals, total;
+    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals;
+    size_t tcount, toff, tfill, test, tlines, cursor, total;
 };
 
 inline Layout3 layout3(long long n_lines, long long n_terms, long long ck_capacity,
@@ -482,6 +748,12 @@ inline Layout3 layout3(long long n_lines, long long n_terms, long long ck_capaci
     L.frame_of_term = off; off = up(off + sizeof(int) * (size_t)n_terms);
     L.keys = off;          off = up(off + sizeof(unsigned long long) * (size_t)table_capacity);
     L.vals = off;          off = up(off + elem * (size_t)table_capacity);
+    L.tcount = off;        off = up(off + sizeof(int) * (size_t)n_terms);
+    L.toff = off;          off = up(off + sizeof(int) * (size_t)n_terms);
+    L.tfill = off;         off = up(off + sizeof(int) * (size_t)n_terms);
+    L.test = off;          off = up(off + sizeof(float) * (size_t)n_terms);
+    L.tlines = off;        off = up(off + sizeof(int) * (size_t)(n_terms > 0 ? n_lines : 0));
+    L.cursor = off;        off = up(off + sizeof(unsigned long long));
     L.total = off;
     return L;
 }
@@ -520,11 +792,80 @@ cudaError_t launch_render3_k(const Render3Args<T> &a, int kernel, T *out, T max_
 
 /* shared by draw and accumulate: frames given per line (int32 frame_of_line or the
  * caller's idxs), accumulate state when mode >= 4 */
+template <typename T, int K, int IN_MAX, int OUT_MAX>
+cudaError_t launch_terms3(const TermArgs<T> &ta, cudaStream_t s)
+{
+    auto fn = term_render3_kernel<T, K, IN_MAX, OUT_MAX>;
+    constexpr size_t smem = term_smem<T>();
+    static std::atomic<int> grid_cache[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int g = grid_cache[dev & 63].load(std::memory_order_relaxed);
+    if (g == 0) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTermThreads, smem);
+        g = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        grid_cache[dev & 63].store(g, std::memory_order_relaxed);
+    }
+    const long long grid = ta.n_terms < g ? ta.n_terms : g;
+    if (grid < 1) return cudaSuccess;
+    fn<<<(unsigned)grid, kTermThreads, smem, s>>>(ta);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+template <typename T, int K>
+cudaError_t launch_terms3_k(const TermArgs<T> &ta, int acc, cudaStream_t s)
+{
+    return acc == kAccMaxSum ? launch_terms3<T, K, 1, 0>(ta, s) : launch_terms3<T, K, 0, 1>(ta, s);
+}
+
+/* the mixed-overlap accumulate: line lists per term, then the shared-memory pass */
+template <typename T>
+cudaError_t run_terms3(const Rec3<T> *recs, const Ck3<T> *cks, Vol v, DevStatus *st, T *out,
+                       T max_val, int kernel, int acc, long long n_lines, long long n_terms,
+                       const int *term_of_line, const int *frame_of_term, unsigned char *ws,
+                       const Layout3 &L, cudaStream_t s)
+{
+    int *tcount = reinterpret_cast<int *>(ws + L.tcount);
+    int *toff = reinterpret_cast<int *>(ws + L.toff);
+    int *tfill = reinterpret_cast<int *>(ws + L.tfill);
+    int *tlines = reinterpret_cast<int *>(ws + L.tlines);
+    float *test = reinterpret_cast<float *>(ws + L.test);
+    unsigned long long *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
+    cudaError_t e = cudaMemsetAsync(tcount, 0, sizeof(int) * (size_t)n_terms, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(test, 0, sizeof(float) * (size_t)n_terms, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    const unsigned nbl = (unsigned)((n_lines + kThreads - 1) / kThreads);
+    const unsigned nbt = (unsigned)((n_terms + kThreads - 1) / kThreads);
+    term_count3_kernel<T><<<nbl, kThreads, 0, s>>>(recs, term_of_line, n_lines, tcount, test);
+    term_offsets_kernel<<<nbt, kThreads, 0, s>>>(tcount, toff, tfill, n_terms, cursor);
+    term_fill3_kernel<T><<<nbl, kThreads, 0, s>>>(recs, term_of_line, n_lines, tfill, tlines);
+    note_launches(3);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    TermArgs<T> ta{recs, cks, v, st, out, max_val, tcount, toff, tlines, frame_of_term, test,
+                   n_terms};
+    switch (kernel) {
+    case CBC_BIWEIGHT:    return launch_terms3_k<T, CBC_BIWEIGHT>(ta, acc, s);
+    case CBC_GAUSSIAN:    return launch_terms3_k<T, CBC_GAUSSIAN>(ta, acc, s);
+    case CBC_PARABOLIC:   return launch_terms3_k<T, CBC_PARABOLIC>(ta, acc, s);
+    case CBC_RECTANGULAR: return launch_terms3_k<T, CBC_RECTANGULAR>(ta, acc, s);
+    default:              return launch_terms3_k<T, CBC_TRIANGULAR>(ta, acc, s);
+    }
+}
+
 template <typename T>
 int run3(T *out, long long n_frames, long long D, long long H, long long W, const T *lines,
          long long n_lines, const void *idxs, int idx_bytes, T max_val, int kernel, int mode,
          unsigned char *ws, const Layout3 &L, long long ck_capacity, long long table_capacity,
-         const int *term_of_line, const int *frame_of_term, cudaStream_t s)
+         const int *term_of_line, const int *frame_of_term, cudaStream_t s,
+         long long n_terms = 0)
 {
     DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
     Rec3<T> *recs = reinterpret_cast<Rec3<T> *>(ws + L.recs);
@@ -544,13 +885,17 @@ int run3(T *out, long long n_frames, long long D, long long H, long long W, cons
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + L.keys);
     T *vals = reinterpret_cast<T *>(ws + L.vals);
     const unsigned long long mask = table_capacity > 0 ? (unsigned long long)table_capacity - 1 : 0;
+    if (mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax) {
+        /* mixed overlaps: every term through shared memory, no global table */
+        if (n_terms > 0) {
+            e = run_terms3<T>(recs, cks, v, st, out, max_val, kernel, mode - 4, n_lines, n_terms,
+                              term_of_line, frame_of_term, ws, L, s);
+            if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+        }
+        return CBC_OK;
+    }
     e = launch_render3_k<T>(a, kernel, out, max_val, mode, term_of_line, keys, vals, mask, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    if (mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax) {
-        e = launch_merge(out, keys, vals, table_capacity, frame_of_term, D * H * W,
-                         mode == 4 + kAccSumMax, st, s);
-        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    }
     return CBC_OK;
 }
 
@@ -616,10 +961,8 @@ int accumulate3_impl(T *out, long long n_frames, long long D, long long H, long 
     if (ck_capacity < 0 || ck_capacity > INT_MAX)
         return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
     const int acc = (in_overlap == CBC_MAX ? 1 : 0) | (out_overlap == CBC_MAX ? 2 : 0);
-    const bool table = acc == kAccMaxSum || acc == kAccSumMax;
-    if (table && (table_capacity < 1 || (table_capacity & (table_capacity - 1))))
-        return fail(CBC_ERR_INVALID, "table_capacity must be a power of two");
-    if (!table) table_capacity = 0;
+    if (table_capacity < 0) return fail(CBC_ERR_INVALID, "table_capacity out of range");
+    table_capacity = 0;            /* the mixed pairs use shared memory, not a table */
     const long long voxels = n_frames * D * H * W;
     if (n_lines > 0 && voxels > 0 && !out) return fail(CBC_ERR_INVALID, "null pointer");
     const Layout3 L = layout3(n_lines, n_terms, ck_capacity, table_capacity, sizeof(T));
@@ -641,12 +984,10 @@ int accumulate3_impl(T *out, long long n_frames, long long D, long long H, long 
     if (n_lines == 0 || voxels == 0) return CBC_OK;
     e = launch_term_frames(terms, term_bytes, frame_of_term, n_lines, n_terms, term_of_line,
                            frame_of_line, st, s);
-    if (e == cudaSuccess && table)
-        e = clear_table(reinterpret_cast<unsigned long long *>(ws + L.keys),
-                        reinterpret_cast<T *>(ws + L.vals), table_capacity, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     return run3<T>(out, n_frames, D, H, W, lines, n_lines, frame_of_line, 4, max_val, kernel,
-                   4 + acc, ws, L, ck_capacity, table_capacity, term_of_line, frame_of_term, s);
+                   4 + acc, ws, L, ck_capacity, table_capacity, term_of_line, frame_of_term, s,
+                   n_terms);
 }
 
 }  // namespace l3

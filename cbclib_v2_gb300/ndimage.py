@@ -653,8 +653,7 @@ def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames,
     elem = 4 if out.dtype == torch.float32 else 8
     lib = _native.lib()
     fn = lib.cbc_accumulate_lines_3d_f32 if elem == 4 else lib.cbc_accumulate_lines_3d_f64
-    table = in_ov != out_ov
-    cap = _table_capacity3(ln) if (table and n_lines) else 0
+    cap = 0          # the mixed pairs build each term's buffer in shared memory
 
     def check(st):
         if st.has(_native.CBC_ERR_INDEX):
@@ -672,16 +671,6 @@ def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames,
     if work is not out:
         out.copy_(work)
     return out
-
-
-def _table_capacity3(ln: torch.Tensor) -> int:
-    """the 3-D analogue of _table_capacity: (long extent + 2w + 3) columns of
-    (3w + 2)^2 voxels"""
-    d = (ln[:, 3:6] - ln[:, 0:3]).abs()
-    w = ln[:, 6].clamp(min=0)
-    est = float(((d.max(dim=1).values + 2 * w + 3) * (3 * w + 2) ** 2).sum().item())
-    need = max(1024, int(2 * est))
-    return 1 << (need - 1).bit_length()
 
 
 def accumulate_lines(out, lines, terms, frames, max_val: float = 1.0,

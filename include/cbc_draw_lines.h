@@ -395,7 +395,9 @@ CBC_API int cbc_draw_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, 
 
 /* accumulate_lines for 3-D lines into volumes (N = 3 of bresenham.cpp:151-259;
  * cuda_draw_lines.cu:1034-1042), with the arguments and status of
- * cbc_accumulate_lines_f32 plus the volume depth. */
+ * cbc_accumulate_lines_f32 plus the volume depth.  The mixed pairs build each term's
+ * buffer in shared memory (in partitions of its voxels when it is large) and need no
+ * table: table_capacity is not used (any value >= 0). */
 CBC_API size_t cbc_accumulate_lines_3d_workspace_size(int64_t n_lines, int64_t n_terms,
                                                       int64_t checkpoint_capacity,
                                                       int64_t table_capacity,
