@@ -12,14 +12,19 @@
  * voxels are visited more than once, and with sum overlap each visit adds, as in the
  * reference.  Here the walk is replayed in the reference's arithmetic: float increments
  * as round-to-nearest intrinsics, and the error terms the reference rounds through
- * double (std::pow(T, int) promotes) evaluated in double on the device.
+ * double (std::pow(T, int) promotes) reproduced bit for bit from float pairs, with a
+ * double fallback near rounding ties (exact.cuh); the float64 overload computes them
+ * in double.  The iterator's per-axis arrays are read and written through constant
+ * indices only (at3 / put3 / increment_at for the line's run-time axes), which keeps
+ * them in registers.
  *
  * Work split: prep3_kernel builds each line's record and walks its long axis once,
- * storing the exact iterator state at every 8th long-axis column inside the volume;
- * render3_kernel then gives every (line, 8-column segment) to one thread, which replays
- * its columns from the checkpoint and combines each drawn voxel into `out` (sum: L2
- * add; max: std::max merge), or, for accumulate_lines, into the (term, voxel) table or
- * directly as in the 2-D path.
+ * storing the exact iterator state at every long-axis column inside the volume;
+ * render3_kernel then gives every (column, quadrant) to one thread, which draws it from
+ * the column's checkpoint and combines each drawn voxel into `out` (sum: L2 add; max:
+ * std::max merge; accumulate_lines with equal overlaps as in the 2-D path).
+ * accumulate_lines with mixed overlaps builds each term in shared memory
+ * (term_render3_kernel below).
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,14 +37,32 @@ namespace cbc {
 namespace l3 {
 
 /* pairs of axes: (0, 1), (0, 2), (1, 2) (UniquePairs<3>, geometry.hpp:403-448) */
-__device__ __constant__ const int kPairA[3] = {0, 0, 1};
-__device__ __constant__ const int kPairB[3] = {1, 2, 2};
+__host__ __device__ constexpr int pair_a(int k) { return k == 2 ? 1 : 0; }
+__host__ __device__ constexpr int pair_b(int k) { return k == 0 ? 1 : 2; }
+
+/* a[i] and a[i] = v for a run-time axis i in [0, 3), written as selects over the three
+ * constant indices: an array indexed only by constants stays in registers, one
+ * indexed at run time is placed in local memory */
+template <typename V>
+__device__ __forceinline__ V at3(const V (&a)[3], int i)
+{
+    return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]);
+}
+
+template <typename V>
+__device__ __forceinline__ void put3(V (&a)[3], int i, V v)
+{
+    #pragma unroll
+    for (int j = 0; j < 3; j++)
+        if (j == i) a[j] = v;
+}
 
 template <typename T>
 struct Rec3 {
     T tau[3];            /* pt1 - pt0                                   */
     T nrm[3][3];         /* normal of pair k, non-zero on its two axes  */
     T len, len2, w, ww;
+    T rlen, rww;         /* RN(1 / len), RN(1 / ww) for the division shortcut */
     int32_t mpt1[3];     /* walk end (the reference adds one step)      */
     int32_t step[3];
     int32_t axis, frame, flags;
@@ -75,7 +98,7 @@ __device__ __forceinline__ void update(const Rec3<T> &r, It3<T> &it)
     for (int i = 0; i < 3; i++) it.next[i] = it.step[i] != 0;
     #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const int a1 = kPairA[k], a2 = kPairB[k];
+        const int a1 = pair_a(k), a2 = pair_b(k);
         if (it.step[a1] && it.step[a2]) {
             const T d1 = it.step[a1] > 0 ? r.nrm[k][a1] : -r.nrm[k][a1];
             const T d2 = it.step[a2] > 0 ? r.nrm[k][a2] : -r.nrm[k][a2];
@@ -101,8 +124,17 @@ __device__ __forceinline__ void increment(const Rec3<T> &r, It3<T> &it, int axis
     it.te = A::add(it.te, x > 0 ? r.tau[axis] : -r.tau[axis]);
     #pragma unroll
     for (int k = 0; k < 3; k++)
-        if (kPairA[k] == axis || kPairB[k] == axis)
+        if (pair_a(k) == axis || pair_b(k) == axis)
             it.ne[k] = A::add(it.ne[k], x > 0 ? r.nrm[k][axis] : -r.nrm[k][axis]);
+}
+
+/* increment() along a run-time axis: the constant-axis step under a predicate */
+template <typename T>
+__device__ __forceinline__ void increment_at(const Rec3<T> &r, It3<T> &it, int axis)
+{
+    #pragma unroll
+    for (int j = 0; j < 3; j++)
+        if (j == axis) increment(r, it, j);
 }
 
 template <typename T>
@@ -121,31 +153,45 @@ __device__ __forceinline__ bool at_end(const Rec3<T> &r, const It3<T> &it)
 }
 
 /* BresenhamPlotter::normal_error (bresenham.hpp:284-289): a T accumulator fed with the
- * double squares of ne / len */
+ * double squares of ne / len.  For float the double steps are reproduced from float
+ * pairs (cbc_normal_error3*, exact.cuh), double arithmetic being a small fraction of
+ * the float rate on this part. */
 template <typename T>
 __device__ __forceinline__ T normal_error(const Rec3<T> &r, const It3<T> &it)
 {
-    using A = Ar<T>;
-    T err = T(0);
-    #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const double b = (double)A::div(it.ne[k], r.len);
-        err = (T)__dadd_rn((double)err, __dmul_rn(b, b));
+    if constexpr (sizeof(T) == sizeof(float)) {
+        return (r.flags & kFastDiv)
+                   ? cbc_normal_error3_r(it.ne[0], it.ne[1], it.ne[2], r.len, r.rlen)
+                   : cbc_normal_error3(it.ne[0], it.ne[1], it.ne[2], r.len);
+    } else {
+        using A = Ar<T>;
+        T err = T(0);
+        #pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double b = (double)A::div(it.ne[k], r.len);
+            err = (T)__dadd_rn((double)err, __dmul_rn(b, b));
+        }
+        return err;
     }
-    return err;
 }
 
-/* BresenhamPlotter::error (bresenham.hpp:291-296) */
+/* BresenhamPlotter::error (bresenham.hpp:291-296) from the position's normal error nf */
 template <typename T>
-__device__ __forceinline__ T error(const Rec3<T> &r, const It3<T> &it)
+__device__ __forceinline__ T error(const Rec3<T> &r, const It3<T> &it, T nf)
 {
-    using A = Ar<T>;
-    const T m1 = -it.te, m2 = A::sub(it.te, r.len2);
-    T ta = m1 < m2 ? m2 : m1;
-    ta = ta < T(0) ? T(0) : ta;
-    const double a = (double)A::div(ta, r.len);
-    const double e = __dadd_rn(__dmul_rn(a, a), (double)normal_error(r, it));
-    return (T)__ddiv_rn(e, (double)r.ww);
+    if constexpr (sizeof(T) == sizeof(float)) {
+        return (r.flags & kFastDiv)
+                   ? cbc_pixel_error_r(it.te, nf, r.len, r.len2, r.ww, r.rlen, r.rww)
+                   : cbc_pixel_error(it.te, nf, r.len, r.len2, r.ww);
+    } else {
+        using A = Ar<T>;
+        const T m1 = -it.te, m2 = A::sub(it.te, r.len2);
+        T ta = m1 < m2 ? m2 : m1;
+        ta = ta < T(0) ? T(0) : ta;
+        const double a = (double)A::div(ta, r.len);
+        const double e = __dadd_rn(__dmul_rn(a, a), (double)nf);
+        return (T)__ddiv_rn(e, (double)r.ww);
+    }
 }
 
 /* BresenhamPlotter construction and begin() (bresenham.hpp:243-263) */
@@ -191,7 +237,7 @@ __device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
     for (int k = 0; k < 3; k++)
         for (int i = 0; i < 3; i++) r.nrm[k][i] = T(0);
     for (int k = 0; k < 3; k++) {
-        const int a1 = kPairA[k], a2 = kPairB[k];
+        const int a1 = pair_a(k), a2 = pair_b(k);
         r.nrm[k][a1] = A::sub(p1[a2], p0[a2]);
         r.nrm[k][a2] = A::sub(p0[a1], p1[a1]);
     }
@@ -209,7 +255,9 @@ __device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
     }
     for (int i = 0; i < 3; i++) { it.cur[i] = mpt0[i]; it.step[i] = r.step[i]; }
     update(r, it);
-    r.flags = kDrawable;
+    r.rlen = A::rcp(r.len);
+    r.rww = A::rcp(r.ww);
+    r.flags = kDrawable | ((A::fast_range(r.len) && A::fast_range(r.ww)) ? kFastDiv : 0);
     return true;
 }
 
@@ -257,7 +305,7 @@ prep3_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lo
                 if (lmin <= lmax) {
                     r.ncols = lmax - lmin + 1;
                     r.c0 = sa > 0 ? lmin : lmax;
-                    nck = (r.ncols + kSeg - 1) / kSeg;
+                    nck = r.ncols;
                 } else {
                     r.flags = 0;
                 }
@@ -289,15 +337,16 @@ prep3_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lo
     }
     if (nck > 0) {
         /* columns are the positions where the next step moves the long axis; one per
-         * long coordinate.  Checkpoint k holds the state at the column of walk index
-         * k * kSeg (walk index = (c - c0) * step of the long axis). */
+         * long coordinate.  Checkpoint k holds the state at the column of walk index k
+         * (walk index = (c - c0) * step of the long axis), so the renders start every
+         * column or quadrant from its own checkpoint without walking. */
         const int ax = r.axis;
         int k = 0;
         long long guard = 0;
         while (k < nck && !at_end(r, it)) {
-            if (it.next[ax]) {
-                const int idx = (it.cur[ax] - r.c0) * sa;
-                if (idx == k * kSeg) {
+            if (at3(it.next, ax)) {
+                const int idx = (at3(it.cur, ax) - r.c0) * sa;
+                if (idx == k) {
                     Ck3<T> c;
                     for (int a = 0; a < 3; a++) c.cur[a] = it.cur[a];
                     c.line = (int32_t)i;
@@ -353,16 +402,16 @@ struct Emit3 {
     }
 };
 
-/* a visited voxel: the error, and for error <= 1 inside the volume, the emit */
+/* a visited voxel with normal error nf: inside the volume and with error <= 1, the emit */
 template <typename T, class EM>
-__device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, const Vol &v,
+__device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, T nf, const Vol &v,
                                       long long fbase, int line, const EM &emit)
 {
-    const T E = error(r, it);
-    if (!(E <= T(1))) return;
     if (it.cur[0] < 0 || it.cur[0] >= v.W || it.cur[1] < 0 || it.cur[1] >= v.H ||
         it.cur[2] < 0 || it.cur[2] >= v.D)
         return;
+    const T E = error(r, it, nf);
+    if (!(E <= T(1))) return;
     const long long vox = ((long long)it.cur[2] * v.H + it.cur[1]) * v.W + it.cur[0];
     emit(fbase, vox, line, E);
 }
@@ -371,45 +420,72 @@ template <typename T>
 __device__ __forceinline__ It3<T> collapse(const Rec3<T> &r, const It3<T> &src, int axis)
 {
     It3<T> it = src;
-    it.step[axis] = 0;
+    put3(it.step, axis, 0);
     update(r, it);
     return it;
 }
 
-/* one column of draw_line_3d (bresenham.hpp:392-428): the centre voxel and the four
- * quadrants of the short-axis plane */
+/* quadrant q of a column of draw_line_3d (bresenham.hpp:404-425): the 2-D walk over the
+ * short-axis plane in the quadrant's directions and the 1-D spans from each of its
+ * voxels; false when the walk ran past its bound (CBC_ERR_RANGE set) */
 template <typename T, class EM>
-__device__ void draw_column(const Rec3<T> &r, const It3<T> &it, const Vol &v, long long fbase,
-                            int line, const EM &emit, DevStatus *st)
+__device__ __forceinline__ bool draw_quadrant(const Rec3<T> &r, const It3<T> &it, int q,
+                                              const Vol &v, long long fbase, int line,
+                                              const EM &emit, DevStatus *st)
 {
     const int ax = r.axis, ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
-    visit(r, it, v, fbase, line, emit);
     long long guard = 0;
-    for (int q = 0; q < 4; q++) {
-        It3<T> ixy = it;
-        ixy.step[ax] = 0;
-        if (q & 1) ixy.step[ax1] = -ixy.step[ax1];
-        if (q >> 1) ixy.step[ax2] = -ixy.step[ax2];
-        update(r, ixy);
-        increment(r, ixy, ((q & 1) ^ (q >> 1)) == 0 ? ax1 : ax2);      /* move */
-        update(r, ixy);
-        for (; normal_error(r, ixy) < r.ww; advance(r, ixy)) {
-            visit(r, ixy, v, fbase, line, emit);
-            for (int j = 1; j < 3; j++) {
-                const int aj = (ax + j) % 3;
-                if (!ixy.next[aj]) continue;
-                It3<T> ix = collapse(r, ixy, aj);
-                for (advance(r, ix); normal_error(r, ix) < r.ww; advance(r, ix)) {
-                    visit(r, ix, v, fbase, line, emit);
-                    if (++guard > 4LL * CBC_MAX_WALK) break;
-                }
-            }
-            if (++guard > 4LL * CBC_MAX_WALK) {
-                atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
-                return;
+    It3<T> ixy = it;
+    put3(ixy.step, ax, 0);
+    if (q & 1) put3(ixy.step, ax1, -at3(ixy.step, ax1));
+    if (q >> 1) put3(ixy.step, ax2, -at3(ixy.step, ax2));
+    update(r, ixy);
+    increment_at(r, ixy, ((q & 1) ^ (q >> 1)) == 0 ? ax1 : ax2);      /* move */
+    update(r, ixy);
+    for (T nxy; (nxy = normal_error(r, ixy)) < r.ww; advance(r, ixy)) {
+        visit(r, ixy, nxy, v, fbase, line, emit);
+        for (int j = 1; j < 3; j++) {
+            const int aj = (ax + j) % 3;
+            if (!at3(ixy.next, aj)) continue;
+            It3<T> ix = collapse(r, ixy, aj);
+            advance(r, ix);
+            for (T nx; (nx = normal_error(r, ix)) < r.ww; advance(r, ix)) {
+                visit(r, ix, nx, v, fbase, line, emit);
+                if (++guard > 4LL * CBC_MAX_WALK) break;
             }
         }
+        if (++guard > 4LL * CBC_MAX_WALK) {
+            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+            return false;
+        }
     }
+    return true;
+}
+
+/* quadrants [q0, q1) of a column of draw_line_3d (bresenham.hpp:392-428), with the
+ * centre voxel when q0 is 0 */
+template <typename T, class EM>
+__device__ __forceinline__ void draw_quadrants(const Rec3<T> &r, const It3<T> &it, int q0,
+                                               int q1, const Vol &v, long long fbase, int line,
+                                               const EM &emit, DevStatus *st)
+{
+    if (q0 == 0) visit(r, it, normal_error(r, it), v, fbase, line, emit);
+    for (int q = q0; q < q1; q++)
+        if (!draw_quadrant(r, it, q, v, fbase, line, emit, st)) return;
+}
+
+/* the iterator at a column from the column's checkpoint */
+template <typename T>
+__device__ __forceinline__ It3<T> column_iter(const Rec3<T> &r, const Ck3<T> &ck)
+{
+    It3<T> it;
+    #pragma unroll
+    for (int i = 0; i < 3; i++) { it.cur[i] = ck.cur[i]; it.step[i] = r.step[i]; }
+    it.te = ck.te;
+    #pragma unroll
+    for (int i = 0; i < 3; i++) it.ne[i] = ck.ne[i];
+    update(r, it);
+    return it;
 }
 
 template <typename T>
@@ -420,39 +496,25 @@ struct Render3Args {
     DevStatus *st;
 };
 
-/* one thread per (line, 8-column segment), grid-stride */
+/* one thread per (column, quadrant), quadrant-major (the lanes of a warp take the same
+ * quadrant of consecutive columns; adjacent lanes on one column's four quadrants would
+ * collide on the voxels the quadrants share), grid-stride; quadrant 0 also takes the
+ * centre voxel */
 template <typename T, int K>
 __global__ void __launch_bounds__(kThreads)
 render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
 {
     if (a.st->flags & kFatal) return;
-    const long long total = (long long)a.st->cks;
+    const long long ncks = (long long)a.st->cks, total = 4 * ncks;
     for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < total;
          item += (long long)gridDim.x * blockDim.x) {
-        const Ck3<T> ck = a.cks[item];
+        const int q = (int)(item / ncks);
+        const Ck3<T> ck = a.cks[item - (long long)q * ncks];
         if (ck.cur[0] == INT_MIN) continue;
         const Rec3<T> r = a.recs[ck.line];
-        It3<T> it;
-        for (int i = 0; i < 3; i++) { it.cur[i] = ck.cur[i]; it.step[i] = r.step[i]; }
-        it.te = ck.te;
-        for (int i = 0; i < 3; i++) it.ne[i] = ck.ne[i];
-        update(r, it);
-        const int ax = r.axis, sa = r.step[ax];
-        const int lo = ck.seg * kSeg, hi = min(lo + kSeg - 1, r.ncols - 1);
+        const It3<T> it = column_iter(r, ck);
         const long long fbase = (long long)r.frame * a.v.D * a.v.H * a.v.W;
-        long long guard = 0;
-        while (!at_end(r, it)) {
-            if (it.next[ax]) {
-                const int idx = (it.cur[ax] - r.c0) * sa;
-                if (idx > hi) break;
-                if (idx >= lo) draw_column(r, it, a.v, fbase, ck.line, emit, a.st);
-            }
-            advance(r, it);
-            if (++guard > 4LL * CBC_MAX_WALK + 64) {
-                atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
-                break;
-            }
-        }
+        draw_quadrants(r, it, q, q + 1, a.v, fbase, ck.line, emit, a.st);
     }
 }
 
@@ -460,8 +522,8 @@ render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
  * A term's lines are combined with in_overlap in a zeroed buffer before the buffer is
  * merged into its frame (bresenham.cpp:151-259).  Here one CTA takes one term at a
  * time and builds that buffer as an open-addressing (voxel, value) table in shared
- * memory: the term's (line, column) items are shared out among the threads, every
- * visited voxel is combined into its slot (in-term max or sum), and afterwards each
+ * memory: the term's columns (and quadrants of columns) are shared out among the
+ * threads, each starting from the column's own checkpoint, every visited voxel is combined into its slot (in-term max or sum), and afterwards each
  * drawn voxel is merged into the volume with one global atomic.  A term with more
  * voxels than the table takes is done in partitions of its voxels (a hash of the voxel
  * index modulo P; each pass walks all of the term's columns and keeps the voxels of
@@ -597,7 +659,7 @@ struct SmEmit {
 };
 
 template <typename T, int K, int IN_MAX, int OUT_MAX>
-__global__ void __launch_bounds__(kTermThreads)
+__global__ void __launch_bounds__(kTermThreads, 3)
 term_render3_kernel(TermArgs<T> a)
 {
     constexpr int kSize = 1 << TermTable<T>::kBits;
@@ -662,42 +724,31 @@ term_render3_kernel(TermArgs<T> a)
                 if (tid == kTermThreads - 1) s_pre[kTermThreads] = before + incl;
                 __syncthreads();
                 const int total = s_pre[nc];
-                /* one (line, column) per item: from the column's segment checkpoint, the
-                 * walk to the column, then the column */
-                for (int j = tid; j < total && !*reinterpret_cast<volatile int *>(&s_full);
+                /* items from the columns' own checkpoints: whole columns while every
+                 * thread has one, then the columns of the last, partial round split into
+                 * their four quadrants (quadrant-major), which shortens that round to
+                 * about a quadrant's time */
+                const int full = total / kTermThreads * kTermThreads, rest = total - full;
+                const int items = full + 4 * rest;
+                for (int j = tid; j < items && !*reinterpret_cast<volatile int *>(&s_full);
                      j += kTermThreads) {
+                    int c = j, q0 = 0, q1 = 4;
+                    if (j >= full) {
+                        q0 = (j - full) / rest;
+                        q1 = q0 + 1;
+                        c = full + (j - full - q0 * rest);
+                    }
                     int lo = 0, hi = nc - 1;
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) >> 1;
-                        if (s_pre[mid] <= j) lo = mid;
+                        if (s_pre[mid] <= c) lo = mid;
                         else hi = mid - 1;
                     }
-                    const int line = s_line[lo], col = j - s_pre[lo];
+                    const int line = s_line[lo], col = c - s_pre[lo];
                     const Rec3<T> r = a.recs[line];
-                    const Ck3<T> ck = a.cks[r.ck_base + col / kSeg];
+                    const Ck3<T> ck = a.cks[r.ck_base + col];
                     if (ck.cur[0] == INT_MIN) continue;
-                    It3<T> it;
-                    for (int i = 0; i < 3; i++) { it.cur[i] = ck.cur[i]; it.step[i] = r.step[i]; }
-                    it.te = ck.te;
-                    for (int i = 0; i < 3; i++) it.ne[i] = ck.ne[i];
-                    update(r, it);
-                    const int ax = r.axis, sa = r.step[ax];
-                    long long guard = 0;
-                    while (!at_end(r, it)) {
-                        if (it.next[ax]) {
-                            const int idx = (it.cur[ax] - r.c0) * sa;
-                            if (idx > col) break;
-                            if (idx == col) {
-                                draw_column(r, it, a.v, 0, line, emit, a.st);
-                                break;
-                            }
-                        }
-                        advance(r, it);
-                        if (++guard > 4LL * CBC_MAX_WALK + 64) {
-                            atomicOr(&a.st->flags, 1 << CBC_ERR_RANGE);
-                            break;
-                        }
-                    }
+                    draw_quadrants(r, column_iter(r, ck), q0, q1, a.v, 0, line, emit, a.st);
                 }
                 __syncthreads();
             }
@@ -872,6 +923,7 @@ int run3(T *out, long long n_frames, long long D, long long H, long long W, cons
     Ck3<T> *cks = reinterpret_cast<Ck3<T> *>(ws + L.cks);
     Vol v{(int)D, (int)H, (int)W};
     const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
+    const bool terms = mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax;
     if (idxs && idx_bytes == 8)
         prep3_kernel<T, int64_t><<<nb, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, v, recs,
                                                          cks, ck_capacity, st);
@@ -885,7 +937,7 @@ int run3(T *out, long long n_frames, long long D, long long H, long long W, cons
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + L.keys);
     T *vals = reinterpret_cast<T *>(ws + L.vals);
     const unsigned long long mask = table_capacity > 0 ? (unsigned long long)table_capacity - 1 : 0;
-    if (mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax) {
+    if (terms) {
         /* mixed overlaps: every term through shared memory, no global table */
         if (n_terms > 0) {
             e = run_terms3<T>(recs, cks, v, st, out, max_val, kernel, mode - 4, n_lines, n_terms,

@@ -64,3 +64,19 @@ void exact_div_batch(const float *a, const float *b, float *out, int64_t n)
 {
     for (int64_t i = 0; i < n; i++) out[i] = cbc_div(a[i], b[i], 1.0f / b[i]);
 }
+
+/* BresenhamPlotter::normal_error of 3-D positions; use_r selects the reciprocal path
+ * (-1 where len is outside its range) */
+void exact_normal_error3_batch(const float *n0, const float *n1, const float *n2,
+                               const float *len, float *out, int64_t n, int use_r)
+{
+    for (int64_t i = 0; i < n; i++) {
+        float l = len[i];
+        if (use_r) {
+            if (!(l >= CBC_DIV_LO && l <= CBC_DIV_HI)) { out[i] = -1.0f; continue; }
+            out[i] = cbc_normal_error3_r(n0[i], n1[i], n2[i], l, 1.0f / l);
+        } else {
+            out[i] = cbc_normal_error3(n0[i], n1[i], n2[i], l);
+        }
+    }
+}

@@ -26,6 +26,7 @@ def exact(tmp_path_factory):
     lib.exact_pixel_error_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_pixel_error_r_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_div_batch.argtypes = [P] * 3 + [ctypes.c_int64]
+    lib.exact_normal_error3_batch.argtypes = [P] * 5 + [ctypes.c_int64, ctypes.c_int]
     lib.exact_take_slow_count.restype = ctypes.c_longlong
     return lib
 
@@ -131,3 +132,63 @@ def test_pixel_error_rarely_leaves_fast_path(exact):
     exact.exact_take_slow_count()
     exact.exact_pixel_error_r_batch(_p(te), _p(ne), _p(ln), _p(w), _p(out), m)
     assert exact.exact_take_slow_count() < 1000     # under 0.1 %
+
+
+def _normal_error3_ref(n0, n1, n2, ln):
+    """the reference's float accumulator: err += std::pow(ne / len, 2) through double"""
+    err = np.zeros(ln.shape, np.float32)
+    for ne in (n0, n1, n2):
+        b = (ne / ln).astype(np.float32)
+        err = (err.astype(np.float64) + b.astype(np.float64) ** 2).astype(np.float32)
+    return err
+
+
+@pytest.mark.parametrize("mode", ['body', 'near_axis', 'wide'])
+def test_normal_error3_bit_exact(exact, mode):
+    """the three-pair normal error of 3-D positions, float(double(err) + b^2) per pair,
+    from float pairs with a double fallback near ties"""
+    rng = np.random.default_rng({'body': 21, 'near_axis': 22, 'wide': 23}[mode])
+    m = 1_000_000
+    ln = (rng.random(m) * 100 + 0.01).astype(np.float32)
+    w = (rng.random(m) * 6 + 0.05).astype(np.float32)
+    ns = [((rng.random(m) * 2 - 1) * w * ln * 1.2).astype(np.float32) for _ in range(3)]
+    if mode == 'near_axis':
+        ns[1] = (ns[1] * 1e-4).astype(np.float32)
+        ns[2][: m // 4] = 0.0
+    if mode == 'wide':
+        e = rng.integers(-40, 40, (3, m))
+        ns = [(ns[k] * 2.0 ** e[k]).astype(np.float32) for k in range(3)]
+    want = _normal_error3_ref(*ns, ln)
+    for use_r in (0, 1):
+        got = np.empty(m, np.float32)
+        exact.exact_take_slow_count()
+        exact.exact_normal_error3_batch(_p(ns[0]), _p(ns[1]), _p(ns[2]), _p(ln), _p(got), m,
+                                        use_r)
+        slow = exact.exact_take_slow_count()
+        fast = got != -1.0 if use_r else np.ones(m, bool)
+        assert fast.mean() > 0.99
+        assert np.array_equal(want[fast].view(np.uint32), got[fast].view(np.uint32))
+        if mode == 'body':
+            assert slow < 2 * m // 1000     # under 0.1 % of the two accumulations
+
+
+def test_normal_error3_ties(exact):
+    """second squares of exactly half an ulp of the accumulator (and one float either
+    side): the double sum sits on or next to a float rounding boundary"""
+    rng = np.random.default_rng(24)
+    m = 200_000
+    n0 = (rng.random(m) * 50 + 0.5).astype(np.float32)
+    err0 = (n0.astype(np.float64) ** 2).astype(np.float32)
+    e = np.frexp(err0)[1].astype(np.int64) - 1            # err0 in [2^e, 2^(e+1))
+    keep = (e - 24) % 2 == 0
+    n0, e = n0[keep], e[keep]
+    half = np.ldexp(np.float32(1.0), ((e - 24) // 2).astype(np.int32)).astype(np.float32)
+    n1 = np.concatenate([half, np.nextafter(half, np.float32(0)),
+                         np.nextafter(half, np.float32(np.inf))]).astype(np.float32)
+    n0 = np.concatenate([n0] * 3)
+    n2 = np.zeros_like(n0)
+    ln = np.ones_like(n0)
+    want = _normal_error3_ref(n0, n1, n2, ln)
+    got = np.empty_like(want)
+    exact.exact_normal_error3_batch(_p(n0), _p(n1), _p(n2), _p(ln), _p(got), n0.size, 1)
+    assert np.array_equal(want.view(np.uint32), got.view(np.uint32))
