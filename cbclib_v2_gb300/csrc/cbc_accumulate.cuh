@@ -71,6 +71,48 @@ __device__ __forceinline__ void table_combine(unsigned long long *keys, T *vals,
     atomicMax(&st->pairs, 4ull * (mask + 1));
 }
 
+/* each term's first slot in the line list: block scan, one cursor atomic per block */
+static __global__ void __launch_bounds__(kThreads)
+term_offsets_kernel(const int *__restrict__ tcount, int *__restrict__ toff,
+                    int *__restrict__ tfill, long long n_terms, unsigned long long *cursor)
+{
+    __shared__ int warp_sums[kThreads / 32];
+    __shared__ unsigned long long block_base;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t < n_terms ? tcount[t] : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int v = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        int sum = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, sum, o);
+            if (lane >= o) sum += u;
+        }
+        if (lane < kThreads / 32) warp_sums[lane] = sum - v;
+        if (lane == kThreads / 32 - 1) block_base = atomicAdd(cursor, (unsigned long long)sum);
+    }
+    __syncthreads();
+    if (t >= n_terms) return;
+    const int o = (int)(block_base + (unsigned long long)(warp_sums[wid] + incl - c));
+    toff[t] = o;
+    tfill[t] = o;
+}
+
+/* the partition of a pixel or voxel index: hash bits independent of the table slot's
+ * (the shared-memory term renders take a term's pixels in partitions) */
+__device__ __forceinline__ unsigned part_hash(unsigned k)
+{
+    unsigned x = k * 0x85ebca6bu;
+    return x ^ (x >> 16);
+}
+
 /* every frames[t] in [0, n_frames) (bresenham.cpp:23-36: "frames range (min, max) is
  * outside of (0, n_frames)"); the int32 copy feeds the merge */
 template <typename FI>
@@ -130,9 +172,12 @@ merge_kernel(T *__restrict__ out, const unsigned long long *__restrict__ keys,
 }
 
 struct AccLayout {
-    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals, total;
+    size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals;
+    size_t tcount, toff, tfill, test, tlines, tbig, counters, total;
 };
 
+/* the counters block after `counters`: the line-list cursor (unsigned long long), the
+ * number of table terms (int) and their estimated pairs (float) */
 inline AccLayout acc_layout(long long n_lines, long long n_terms, long long ck_capacity,
                      long long table_capacity, size_t rec_bytes, size_t ck_bytes, size_t elem)
 {
@@ -147,6 +192,13 @@ inline AccLayout acc_layout(long long n_lines, long long n_terms, long long ck_c
     L.frame_of_term = off; off = up(off + sizeof(int) * (size_t)n_terms);
     L.keys = off;          off = up(off + sizeof(unsigned long long) * (size_t)table_capacity);
     L.vals = off;          off = up(off + elem * (size_t)table_capacity);
+    L.tcount = off;        off = up(off + sizeof(int) * (size_t)n_terms);
+    L.toff = off;          off = up(off + sizeof(int) * (size_t)n_terms);
+    L.tfill = off;         off = up(off + sizeof(int) * (size_t)n_terms);
+    L.test = off;          off = up(off + sizeof(float) * (size_t)n_terms);
+    L.tlines = off;        off = up(off + sizeof(int) * (size_t)(n_terms > 0 ? n_lines : 0));
+    L.tbig = off;          off = up(off + sizeof(int) * (size_t)n_terms);
+    L.counters = off;      off = up(off + 16);
     L.total = off;
     return L;
 }

@@ -11,6 +11,7 @@
 #include <limits.h>
 #include <atomic>
 #include <string>
+#include <type_traits>
 
 #include "cbc_draw_lines.h"
 #include "exact.cuh"
@@ -853,6 +854,11 @@ struct PixelRing {
     unsigned char slot[kRing];     /* owner lane of each pixel */
 };
 
+/* actions that draw only some lines define keep_line(line) */
+template <class A, class = void> struct FiltersLines : std::false_type {};
+template <class A>
+struct FiltersLines<A, std::void_t<decltype(&A::keep_line)>> : std::true_type {};
+
 template <typename T, class Act>
 __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
 {
@@ -962,7 +968,9 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
         bool cols = false;             /* columns of this item left to find */
         if (item < total) {
             const Checkpoint<T> ck = a.cks[item];
-            if (ck.cx != INT_MIN) {
+            bool keep = true;
+            if constexpr (FiltersLines<Act>::value) keep = act.keep_line(ck.line);
+            if (ck.cx != INT_MIN && keep) {
                 const LineRec<T> r = a.recs[ck.line];
                 ax = r.flags & kAxisY;
                 wk.init(r);

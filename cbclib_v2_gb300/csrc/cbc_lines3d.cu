@@ -571,40 +571,6 @@ term_count3_kernel(const Rec3<T> *__restrict__ recs, const int *__restrict__ ter
     atomicAdd(&test[t], (float)recs[i].ncols * 3.14159265f * r * r);
 }
 
-/* each term's first slot in the line list: block scan, one cursor atomic per block */
-__global__ void __launch_bounds__(kThreads)
-term_offsets_kernel(const int *__restrict__ tcount, int *__restrict__ toff,
-                    int *__restrict__ tfill, long long n_terms, unsigned long long *cursor)
-{
-    __shared__ int warp_sums[kThreads / 32];
-    __shared__ unsigned long long block_base;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int c = t < n_terms ? tcount[t] : 0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = c;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) warp_sums[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-        const int v = lane < kThreads / 32 ? warp_sums[lane] : 0;
-        int sum = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, sum, o);
-            if (lane >= o) sum += u;
-        }
-        if (lane < kThreads / 32) warp_sums[lane] = sum - v;
-        if (lane == kThreads / 32 - 1) block_base = atomicAdd(cursor, (unsigned long long)sum);
-    }
-    __syncthreads();
-    if (t >= n_terms) return;
-    const int o = (int)(block_base + (unsigned long long)(warp_sums[wid] + incl - c));
-    toff[t] = o;
-    tfill[t] = o;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 term_fill3_kernel(const Rec3<T> *__restrict__ recs, const int *__restrict__ term_of_line,
@@ -613,13 +579,6 @@ term_fill3_kernel(const Rec3<T> *__restrict__ recs, const int *__restrict__ term
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_lines || recs[i].ncols <= 0) return;
     tlines[atomicAdd(&tfill[term_of_line[i]], 1)] = (int)i;
-}
-
-/* the partition of a voxel: hash bits independent of the table slot's */
-__device__ __forceinline__ unsigned voxel_part(int k)
-{
-    unsigned x = (unsigned)k * 0x85ebca6bu;
-    return x ^ (x >> 16);
 }
 
 /* a term's voxels of the current partition into the shared table; `count` grows with
@@ -636,7 +595,7 @@ struct SmEmit {
         using A = Ar<T>;
         constexpr int kBits = TermTable<T>::kBits, kSize = 1 << kBits;
         const int k = (int)vox;
-        if ((voxel_part(k) & pmask) != part) return;
+        if ((part_hash((unsigned)k) & pmask) != part) return;
         if (*reinterpret_cast<volatile int *>(full)) return;    /* this pass is redone */
         const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
         unsigned h = ((unsigned)k * 2654435761u) >> (32 - kBits);   /* Fibonacci hashing */

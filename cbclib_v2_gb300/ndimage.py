@@ -565,16 +565,6 @@ def _as_device_ints(a, name: str, dev: torch.device) -> torch.Tensor:
     return t.to(device=dev).contiguous()
 
 
-def _table_capacity(ln: torch.Tensor) -> int:
-    """A power of two about twice an upper estimate of the (line, pixel) pairs the
-    lines draw: (long extent + 2w + 3) columns of (3w + 2) pixels each."""
-    d = (ln[:, 2:4] - ln[:, 0:2]).abs()
-    w = ln[:, 4].clamp(min=0)
-    est = float(((d.max(dim=1).values + 2 * w + 3) * (3 * w + 2)).sum().item())
-    need = max(1024, int(2 * est))
-    return 1 << (need - 1).bit_length()
-
-
 def _accumulate_lines_cuda(out: torch.Tensor, lines, terms, frames, max_val: float, kernel: int,
                            in_ov: int, out_ov: int) -> torch.Tensor:
     dev = out.device
@@ -600,7 +590,9 @@ def _accumulate_lines_cuda(out: torch.Tensor, lines, terms, frames, max_val: flo
         with _ws_lock:
             ws = _workspaces.setdefault(key, Workspace(dev))
         ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
-        table_cap = max(ws.capacity, _table_capacity(ln)) if (table and n_lines) else 0
+        # terms built in shared memory need no table; the call names the capacity its
+        # largest terms need (CBC_ERR_CAPACITY, pairs_needed) and is run again
+        table_cap = ws.capacity if (table and n_lines) else 0
         for _ in range(6):
             nbytes = lib.cbc_accumulate_lines_workspace_size(n_lines, n_terms, ck_capacity,
                                                              table_cap, elem)

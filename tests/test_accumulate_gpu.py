@@ -136,23 +136,54 @@ def test_errors(cuda):
 
 
 def test_small_table_reports_capacity_and_draws_nothing(cuda):
-    """through the C ABI: a hash table too small for the call sets CBC_ERR_CAPACITY,
-    names a larger capacity and leaves out untouched"""
-    shape, lines, terms, frames = _case(17, n=200, n_terms=10)
+    """through the C ABI: terms too large for shared memory (two of 300 lines) need the
+    workspace table; a table too small for them sets CBC_ERR_CAPACITY, names a larger
+    capacity and leaves out untouched"""
+    n, n_terms = 600, 2
+    shape, lines, terms, frames = _case(17, n=n, n_terms=n_terms)
     lib = _native.lib()
     out = torch.zeros(shape, device='cuda')
     ln = torch.from_numpy(lines).cuda()
     tm = torch.from_numpy(terms.astype(np.int64)).cuda()
     fr = torch.from_numpy(frames.astype(np.int64)).cuda()
-    ck, cap = 16 * 200 + 1024, 1024
-    nbytes = lib.cbc_accumulate_lines_workspace_size(200, 10, ck, cap, 4)
-    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
     stream = torch.cuda.current_stream().cuda_stream
-    rc = lib.cbc_accumulate_lines_f32(out.data_ptr(), *shape, ln.data_ptr(), 200, tm.data_ptr(),
-                                      8, fr.data_ptr(), 8, 10, 1.0, _native.KERNELS['rectangular'],
-                                      1, 0, ws.data_ptr(), nbytes, ck, cap, stream)
-    assert rc == 0
-    st = _native.Status()
-    assert lib.cbc_read_status(ws.data_ptr(), ctypes.byref(st), stream) == 0
-    assert st.has(_native.CBC_ERR_CAPACITY) and st.pairs_needed > cap
-    assert not out.any()
+    for cap in (0, 1024):
+        ck = 16 * n + 1024
+        nbytes = lib.cbc_accumulate_lines_workspace_size(n, n_terms, ck, cap, 4)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+        rc = lib.cbc_accumulate_lines_f32(out.data_ptr(), *shape, ln.data_ptr(), n,
+                                          tm.data_ptr(), 8, fr.data_ptr(), 8, n_terms, 1.0,
+                                          _native.KERNELS['rectangular'], 1, 0, ws.data_ptr(),
+                                          nbytes, ck, cap, stream)
+        assert rc == 0
+        st = _native.Status()
+        assert lib.cbc_read_status(ws.data_ptr(), ctypes.byref(st), stream) == 0
+        assert st.has(_native.CBC_ERR_CAPACITY) and st.pairs_needed > cap
+        assert not out.any()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("mode", [('max', 'sum'), ('sum', 'max')])
+def test_mixed_term_sizes(cuda, dtype, mode):
+    """terms of 1 to 400 lines in one call: small terms in one shared-memory pass,
+    larger ones in several partitions, the largest through the workspace table (the
+    host retries with the capacity the first call names)"""
+    rng = np.random.default_rng(29)
+    F, H, W = 2, 160, 200
+    sizes = [1, 2, 3, 5, 8, 13, 40, 90, 400, 1, 7, 250]
+    terms = np.repeat(np.arange(len(sizes)), sizes)
+    n = terms.size
+    frames = rng.integers(0, F, len(sizes))
+    # each term's lines cluster around a centre, so they overlap one another
+    centre = rng.random((len(sizes), 2)) * [W, H]
+    p0 = centre[terms] + rng.normal(scale=25, size=(n, 2))
+    v = rng.normal(size=(n, 2))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    p1 = p0 + v * rng.uniform(5, 60, n)[:, None]
+    lines = np.concatenate([p0, p1, rng.uniform(0.5, 4, (n, 1))], axis=1).astype(dtype)
+    perm = rng.permutation(n)
+    lines, terms = lines[perm], terms[perm]
+    ref, got = _run_both((F, H, W), lines, terms, frames, 2.0, 'triangular', *mode, dtype)
+    np.testing.assert_allclose(got, ref, **_tol(dtype, 2.0))
+    ws = next(w for k, w in ndimage._workspaces.items() if k[0] == 'accumulate')
+    assert ws.capacity > 0                      # the largest terms went through the table
