@@ -106,16 +106,7 @@ accumulate_kernel(AccArgs<T> a)
     act.st = a.d.st;
     if constexpr (MODE == kAccMaxSum || MODE == kAccSumMax) {
         /* only the large terms, into a table at most half full by their estimate */
-        if (*a.nbig == 0) return;
-        unsigned long long need = 1024;
-        while ((float)need < 2.0f * *a.big_est && need < (1ull << 40)) need <<= 1;
-        if ((unsigned long long)a.table_capacity < need) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                atomicOr(&a.d.st->flags, 1 << CBC_ERR_CAPACITY);
-                atomicMax(&a.d.st->pairs, need);
-            }
-            return;
-        }
+        if (!table_terms_fit(a.nbig, a.big_est, a.table_capacity, a.d.st)) return;
     }
     drive_segments(a.d, act);
 }
@@ -148,8 +139,8 @@ cudaError_t launch_accumulate(const AccArgs<T> &a, int mode, cudaStream_t s)
 
 /* ---- mixed overlaps: terms built in shared memory ---------------------------------- */
 template <typename T> struct Term2Table { static constexpr int kBits = 12; };   /* 4096 slots */
-constexpr int kTerm2Threads = 128;
-constexpr int kTerm2Blocks = 5;         /* resident CTAs per SM the budgets target    */
+constexpr int kTerm2Threads = 256;
+constexpr int kTerm2Blocks = 3;         /* resident CTAs per SM the budgets target    */
 constexpr int kTerm2Stack = 64;         /* pending partitions per term                */
 constexpr int kTerm2MaxParts = 8;       /* larger terms use the workspace table       */
 constexpr float kTerm2Fill = 0.6f;      /* planned fill of the table per partition    */
@@ -204,23 +195,6 @@ term_fill2_kernel(const LineRec<T> *__restrict__ recs, const int *__restrict__ t
     const LineRec<T> &r = recs[i];
     if (!(r.flags & kDrawable) || r.ncols <= 0) return;
     tlines[atomicAdd(&tfill[term_of_line[i]], 1)] = (int)i;
-}
-
-/* terms whose estimate needs more than kTerm2MaxParts partitions go through the
- * workspace table; their count and estimated pairs size it */
-static __global__ void __launch_bounds__(kThreads)
-term_class2_kernel(const int *__restrict__ tcount, const float *__restrict__ test,
-                   long long n_terms, float limit, int *__restrict__ tbig, int *nbig,
-                   float *big_est)
-{
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_terms) return;
-    const bool big = tcount[t] > 0 && test[t] > limit;
-    tbig[t] = big ? 1 : 0;
-    if (big) {
-        atomicAdd(nbig, 1);
-        atomicAdd(big_est, test[t]);
-    }
 }
 
 /* one term partition's pixels into the CTA's table: claim a slot (recording it in the
@@ -569,7 +543,7 @@ int accumulate_impl(T *out, long long n_frames, long long H, long long W, const 
         term_count2_kernel<T><<<nb, kThreads, 0, s>>>(recs, term_of_line, n_lines, tcount, test);
         term_offsets_kernel<<<nbt, kThreads, 0, s>>>(tcount, toff, tfill, n_terms, cursor);
         term_fill2_kernel<T><<<nb, kThreads, 0, s>>>(recs, term_of_line, n_lines, tfill, tlines);
-        term_class2_kernel<<<nbt, kThreads, 0, s>>>(
+        term_class_kernel<<<nbt, kThreads, 0, s>>>(
             tcount, test, n_terms,
             (float)kTerm2MaxParts * kTerm2Fill * (float)(1 << Term2Table<T>::kBits), tbig, nbig,
             big_est);

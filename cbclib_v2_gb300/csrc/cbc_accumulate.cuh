@@ -105,6 +105,42 @@ term_offsets_kernel(const int *__restrict__ tcount, int *__restrict__ toff,
     tfill[t] = o;
 }
 
+/* terms whose pixel estimate exceeds `limit` (more partitions of a shared-memory
+ * table than the term renders take) go through the workspace table; their count and
+ * estimated pairs size it */
+static __global__ void __launch_bounds__(kThreads)
+term_class_kernel(const int *__restrict__ tcount, const float *__restrict__ test,
+                   long long n_terms, float limit, int *__restrict__ tbig, int *nbig,
+                   float *big_est)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_terms) return;
+    const bool big = tcount[t] > 0 && test[t] > limit;
+    tbig[t] = big ? 1 : 0;
+    if (big) {
+        atomicAdd(nbig, 1);
+        atomicAdd(big_est, test[t]);
+    }
+}
+
+/* whether the table pass has work: false when no term goes through the workspace
+ * table, or when the table holds fewer than twice their estimated pairs (rounded up to
+ * a power of two, at least 1024); the latter sets CBC_ERR_CAPACITY with that capacity
+ * as pairs_needed, so the call draws nothing and can be retried */
+__device__ __forceinline__ bool table_terms_fit(const int *nbig, const float *big_est,
+                                                long long capacity, DevStatus *st)
+{
+    if (*nbig == 0) return false;
+    unsigned long long need = 1024;
+    while ((float)need < 2.0f * *big_est && need < (1ull << 40)) need <<= 1;
+    if ((unsigned long long)capacity >= need) return true;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicOr(&st->flags, 1 << CBC_ERR_CAPACITY);
+        atomicMax(&st->pairs, need);
+    }
+    return false;
+}
+
 /* the partition of a pixel or voxel index: hash bits independent of the table slot's
  * (the shared-memory term renders take a term's pixels in partitions) */
 __device__ __forceinline__ unsigned part_hash(unsigned k)

@@ -389,7 +389,11 @@ struct Emit3 {
     unsigned long long *keys;
     T *vals;
     unsigned long long mask;
+    const int *tbig;               /* mixed overlaps: the terms this pass draws */
     DevStatus *st;
+    __device__ __forceinline__ bool table_mode() const {
+        return mode == 4 + kAccMaxSum || mode == 4 + kAccSumMax;
+    }
     __device__ __forceinline__ void operator()(long long fbase, long long vox, int line, T E) const {
         using A = Ar<T>;
         const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
@@ -397,6 +401,12 @@ struct Emit3 {
         case 0:  atomicAdd(out + fbase + vox, v); break;
         case 1:  global_combine_max(out + fbase + vox, v); break;
         case 4 + kAccSumSum: atomicAdd(out + fbase + vox, v); break;
+        case 4 + kAccMaxSum:
+            table_combine<T, 1>(keys, vals, mask, term_of_line[line], vox, v, st);
+            break;
+        case 4 + kAccSumMax:
+            table_combine<T, 0>(keys, vals, mask, term_of_line[line], vox, v, st);
+            break;
         default:  global_combine_max(out + fbase + vox, T(0) < v ? v : T(0)); break;
         }
     }
@@ -494,6 +504,9 @@ struct Render3Args {
     const Ck3<T> *cks;
     Vol v;
     DevStatus *st;
+    const int *nbig;               /* mixed overlaps: terms through the workspace table */
+    const float *big_est;          /* and their estimated pairs                        */
+    long long table_capacity;
 };
 
 /* one thread per (column, quadrant), quadrant-major (the lanes of a warp take the same
@@ -501,16 +514,19 @@ struct Render3Args {
  * collide on the voxels the quadrants share), grid-stride; quadrant 0 also takes the
  * centre voxel */
 template <typename T, int K>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
 {
     if (a.st->flags & kFatal) return;
+    const bool table = emit.table_mode();
+    if (table && !table_terms_fit(a.nbig, a.big_est, a.table_capacity, a.st)) return;
     const long long ncks = (long long)a.st->cks, total = 4 * ncks;
     for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < total;
          item += (long long)gridDim.x * blockDim.x) {
         const int q = (int)(item / ncks);
         const Ck3<T> ck = a.cks[item - (long long)q * ncks];
         if (ck.cur[0] == INT_MIN) continue;
+        if (table && !emit.tbig[emit.term_of_line[ck.line]]) continue;
         const Rec3<T> r = a.recs[ck.line];
         const It3<T> it = column_iter(r, ck);
         const long long fbase = (long long)r.frame * a.v.D * a.v.H * a.v.W;
@@ -528,13 +544,16 @@ render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
  * voxels than the table takes is done in partitions of its voxels (a hash of the voxel
  * index modulo P; each pass walks all of the term's columns and keeps the voxels of
  * one partition): P starts from an estimate, and a partition that fills the table is
- * split in two and redone, so every voxel is merged exactly once and there is no
- * capacity to run out of. */
+ * split in two and redone, so every voxel is merged exactly once.  Terms whose estimate
+ * needs more than kTermMaxParts partitions go instead through the workspace (term,
+ * voxel) table in render3_kernel, sized by the call (CBC_ERR_CAPACITY names the
+ * capacity to retry with). */
 template <typename T> struct TermTable { static constexpr int kBits = 13; };   /* 64 KB */
 template <> struct TermTable<double> { static constexpr int kBits = 12; };       /* 48 KB */
 constexpr int kTermThreads = 256;
 constexpr int kTermChunk = kTermThreads;      /* lines staged per chunk */
 constexpr int kTermStack = 64;                /* pending partitions per term */
+constexpr int kTermMaxParts = 8;              /* larger terms use the workspace table */
 
 template <typename T>
 struct TermArgs {
@@ -544,7 +563,7 @@ struct TermArgs {
     DevStatus *st;
     T *out;
     T max_val;
-    const int *tcount, *toff, *tlines, *frame_of_term;
+    const int *tcount, *toff, *tlines, *tbig, *frame_of_term;
     const float *test;
     long long n_terms;
 };
@@ -635,14 +654,14 @@ term_render3_kernel(TermArgs<T> a)
     const long long frame_vox = (long long)a.v.D * a.v.H * a.v.W;
     for (long long t = blockIdx.x; t < a.n_terms; t += gridDim.x) {
         const int n_t = a.tcount[t];
-        if (n_t == 0) continue;
+        if (n_t == 0 || a.tbig[t]) continue;
         /* pending partitions (part, log2 P), one per 32-bit word */
         if (tid == 0) {
-            /* at most 32 starting partitions: with one more entry per split, the stack
-             * stays below 32 + 24 entries */
+            /* at most kTermMaxParts starting partitions: with one more entry per split,
+             * the stack stays below kTermMaxParts + 24 entries */
             const float want = a.test[t] / (0.6f * (float)kSize);
             int lg = 0;
-            while ((float)(1 << lg) < want && lg < 5) lg++;
+            while ((float)(1 << lg) < want && (1 << lg) < kTermMaxParts) lg++;
             s_depth = 0;
             for (int p = (1 << lg) - 1; p >= 0; p--) s_stack[s_depth++] = ((unsigned)p << 5) | lg;
         }
@@ -739,7 +758,7 @@ term_render3_kernel(TermArgs<T> a)
 
 struct Layout3 {
     size_t status, recs, cks, frame_of_line, term_of_line, frame_of_term, keys, vals;
-    size_t tcount, toff, tfill, test, tlines, cursor, total;
+    size_t tcount, toff, tfill, test, tlines, tbig, counters, total;
 };
 
 inline Layout3 layout3(long long n_lines, long long n_terms, long long ck_capacity,
@@ -763,7 +782,8 @@ inline Layout3 layout3(long long n_lines, long long n_terms, long long ck_capaci
     L.tfill = off;         off = up(off + sizeof(int) * (size_t)n_terms);
     L.test = off;          off = up(off + sizeof(float) * (size_t)n_terms);
     L.tlines = off;        off = up(off + sizeof(int) * (size_t)(n_terms > 0 ? n_lines : 0));
-    L.cursor = off;        off = up(off + sizeof(unsigned long long));
+    L.tbig = off;          off = up(off + sizeof(int) * (size_t)n_terms);
+    L.counters = off;      off = up(off + 16);    /* cursor, table terms, their pairs */
     L.total = off;
     return L;
 }
@@ -780,11 +800,11 @@ cudaError_t launch_render3(const Render3Args<T> &a, const Emit3<T, K> &emit, cud
 template <typename T>
 cudaError_t launch_render3_k(const Render3Args<T> &a, int kernel, T *out, T max_val, int mode,
                              const int *term_of_line, unsigned long long *keys, T *vals,
-                             unsigned long long mask, cudaStream_t s)
+                             unsigned long long mask, const int *tbig, cudaStream_t s)
 {
 #define CBC_L3_CASE(KK)                                                                  \
     case KK: {                                                                           \
-        Emit3<T, KK> e{out, max_val, mode, term_of_line, keys, vals, mask, a.st};        \
+        Emit3<T, KK> e{out, max_val, mode, term_of_line, keys, vals, mask, tbig, a.st};  \
         return launch_render3<T, KK>(a, e, s);                                           \
     }
     switch (kernel) {
@@ -793,7 +813,8 @@ cudaError_t launch_render3_k(const Render3Args<T> &a, int kernel, T *out, T max_
     CBC_L3_CASE(CBC_PARABOLIC)
     CBC_L3_CASE(CBC_RECTANGULAR)
     default: {
-        Emit3<T, CBC_TRIANGULAR> e{out, max_val, mode, term_of_line, keys, vals, mask, a.st};
+        Emit3<T, CBC_TRIANGULAR> e{out, max_val, mode, term_of_line, keys, vals, mask, tbig,
+                                    a.st};
         return launch_render3<T, CBC_TRIANGULAR>(a, e, s);
     }
     }
@@ -834,40 +855,62 @@ cudaError_t launch_terms3_k(const TermArgs<T> &ta, int acc, cudaStream_t s)
     return acc == kAccMaxSum ? launch_terms3<T, K, 1, 0>(ta, s) : launch_terms3<T, K, 0, 1>(ta, s);
 }
 
-/* the mixed-overlap accumulate: line lists per term, then the shared-memory pass */
+/* the mixed-overlap accumulate: line lists per term; the terms too large for shared
+ * memory through the workspace table (render3_kernel's table modes, then the merge),
+ * the others in shared memory */
 template <typename T>
-cudaError_t run_terms3(const Rec3<T> *recs, const Ck3<T> *cks, Vol v, DevStatus *st, T *out,
-                       T max_val, int kernel, int acc, long long n_lines, long long n_terms,
-                       const int *term_of_line, const int *frame_of_term, unsigned char *ws,
-                       const Layout3 &L, cudaStream_t s)
+cudaError_t run_terms3(const Render3Args<T> &ra, T *out, T max_val, int kernel, int acc,
+                       long long n_lines, long long n_terms, const int *term_of_line,
+                       const int *frame_of_term, unsigned long long *keys, T *vals,
+                       long long table_capacity, unsigned char *ws, const Layout3 &L,
+                       cudaStream_t s)
 {
     int *tcount = reinterpret_cast<int *>(ws + L.tcount);
     int *toff = reinterpret_cast<int *>(ws + L.toff);
     int *tfill = reinterpret_cast<int *>(ws + L.tfill);
     int *tlines = reinterpret_cast<int *>(ws + L.tlines);
+    int *tbig = reinterpret_cast<int *>(ws + L.tbig);
     float *test = reinterpret_cast<float *>(ws + L.test);
-    unsigned long long *cursor = reinterpret_cast<unsigned long long *>(ws + L.cursor);
+    unsigned long long *cursor = reinterpret_cast<unsigned long long *>(ws + L.counters);
+    int *nbig = reinterpret_cast<int *>(ws + L.counters + 8);
+    float *big_est = reinterpret_cast<float *>(ws + L.counters + 12);
     cudaError_t e = cudaMemsetAsync(tcount, 0, sizeof(int) * (size_t)n_terms, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(test, 0, sizeof(float) * (size_t)n_terms, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ws + L.counters, 0, 16, s);
+    if (e == cudaSuccess && table_capacity > 0) e = clear_table(keys, vals, table_capacity, s);
     if (e != cudaSuccess) return e;
     const unsigned nbl = (unsigned)((n_lines + kThreads - 1) / kThreads);
     const unsigned nbt = (unsigned)((n_terms + kThreads - 1) / kThreads);
-    term_count3_kernel<T><<<nbl, kThreads, 0, s>>>(recs, term_of_line, n_lines, tcount, test);
+    term_count3_kernel<T><<<nbl, kThreads, 0, s>>>(ra.recs, term_of_line, n_lines, tcount, test);
     term_offsets_kernel<<<nbt, kThreads, 0, s>>>(tcount, toff, tfill, n_terms, cursor);
-    term_fill3_kernel<T><<<nbl, kThreads, 0, s>>>(recs, term_of_line, n_lines, tfill, tlines);
-    note_launches(3);
+    term_fill3_kernel<T><<<nbl, kThreads, 0, s>>>(ra.recs, term_of_line, n_lines, tfill, tlines);
+    term_class_kernel<<<nbt, kThreads, 0, s>>>(
+        tcount, test, n_terms, (float)kTermMaxParts * 0.6f * (float)(1 << TermTable<T>::kBits),
+        tbig, nbig, big_est);
+    note_launches(4);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    TermArgs<T> ta{recs, cks, v, st, out, max_val, tcount, toff, tlines, frame_of_term, test,
-                   n_terms};
+    Render3Args<T> a = ra;
+    a.nbig = nbig;
+    a.big_est = big_est;
+    a.table_capacity = table_capacity;
+    const unsigned long long mask = table_capacity > 0 ? (unsigned long long)table_capacity - 1 : 0;
+    e = launch_render3_k<T>(a, kernel, out, max_val, 4 + acc, term_of_line, keys, vals, mask,
+                            tbig, s);
+    if (e != cudaSuccess) return e;
+    TermArgs<T> ta{ra.recs, ra.cks, ra.v, ra.st, out, max_val, tcount, toff, tlines, tbig,
+                   frame_of_term, test, n_terms};
     switch (kernel) {
-    case CBC_BIWEIGHT:    return launch_terms3_k<T, CBC_BIWEIGHT>(ta, acc, s);
-    case CBC_GAUSSIAN:    return launch_terms3_k<T, CBC_GAUSSIAN>(ta, acc, s);
-    case CBC_PARABOLIC:   return launch_terms3_k<T, CBC_PARABOLIC>(ta, acc, s);
-    case CBC_RECTANGULAR: return launch_terms3_k<T, CBC_RECTANGULAR>(ta, acc, s);
-    default:              return launch_terms3_k<T, CBC_TRIANGULAR>(ta, acc, s);
+    case CBC_BIWEIGHT:    e = launch_terms3_k<T, CBC_BIWEIGHT>(ta, acc, s); break;
+    case CBC_GAUSSIAN:    e = launch_terms3_k<T, CBC_GAUSSIAN>(ta, acc, s); break;
+    case CBC_PARABOLIC:   e = launch_terms3_k<T, CBC_PARABOLIC>(ta, acc, s); break;
+    case CBC_RECTANGULAR: e = launch_terms3_k<T, CBC_RECTANGULAR>(ta, acc, s); break;
+    default:              e = launch_terms3_k<T, CBC_TRIANGULAR>(ta, acc, s); break;
     }
+    if (e == cudaSuccess && table_capacity > 0)
+        e = launch_merge(out, keys, vals, table_capacity, frame_of_term,
+                         (long long)ra.v.D * ra.v.H * ra.v.W, acc == kAccSumMax, ra.st, s);
+    return e;
 }
 
 template <typename T>
@@ -892,20 +935,18 @@ int run3(T *out, long long n_frames, long long D, long long H, long long W, cons
     note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    Render3Args<T> a{recs, cks, v, st};
+    Render3Args<T> a{recs, cks, v, st, nullptr, nullptr, 0};
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + L.keys);
     T *vals = reinterpret_cast<T *>(ws + L.vals);
-    const unsigned long long mask = table_capacity > 0 ? (unsigned long long)table_capacity - 1 : 0;
     if (terms) {
-        /* mixed overlaps: every term through shared memory, no global table */
         if (n_terms > 0) {
-            e = run_terms3<T>(recs, cks, v, st, out, max_val, kernel, mode - 4, n_lines, n_terms,
-                              term_of_line, frame_of_term, ws, L, s);
+            e = run_terms3<T>(a, out, max_val, kernel, mode - 4, n_lines, n_terms, term_of_line,
+                              frame_of_term, keys, vals, table_capacity, ws, L, s);
             if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
         }
         return CBC_OK;
     }
-    e = launch_render3_k<T>(a, kernel, out, max_val, mode, term_of_line, keys, vals, mask, s);
+    e = launch_render3_k<T>(a, kernel, out, max_val, mode, term_of_line, keys, vals, 0, nullptr, s);
     if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
     return CBC_OK;
 }
@@ -972,8 +1013,10 @@ int accumulate3_impl(T *out, long long n_frames, long long D, long long H, long 
     if (ck_capacity < 0 || ck_capacity > INT_MAX)
         return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
     const int acc = (in_overlap == CBC_MAX ? 1 : 0) | (out_overlap == CBC_MAX ? 2 : 0);
-    if (table_capacity < 0) return fail(CBC_ERR_INVALID, "table_capacity out of range");
-    table_capacity = 0;            /* the mixed pairs use shared memory, not a table */
+    const bool table = acc == kAccMaxSum || acc == kAccSumMax;
+    if (table && (table_capacity < 0 || (table_capacity & (table_capacity - 1))))
+        return fail(CBC_ERR_INVALID, "table_capacity must be 0 or a power of two");
+    if (!table) table_capacity = 0;
     const long long voxels = n_frames * D * H * W;
     if (n_lines > 0 && voxels > 0 && !out) return fail(CBC_ERR_INVALID, "null pointer");
     const Layout3 L = layout3(n_lines, n_terms, ck_capacity, table_capacity, sizeof(T));

@@ -107,10 +107,11 @@ def _volumes_of(out: torch.Tensor):
 
 
 def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
-          table_cap: int = 0, on_status=None) -> None:
+          table: bool = False, on_status=None) -> None:
     """Run a 3-D library call ``call(buf, ck_capacity, table_capacity, stream)`` with
     this thread's workspace, raise the status' errors and retry with more room when the
-    call reports that its checkpoints or its table did not fit."""
+    call reports that its checkpoints or (``table``: mixed-overlap accumulate) its
+    workspace table did not fit."""
     lib = _native.lib()
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev)
@@ -118,7 +119,7 @@ def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
         with _ws_lock:
             ws = _workspaces.setdefault(key, Workspace(dev))
         ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
-        table_cap = max(ws.capacity, table_cap) if table_cap else 0
+        table_cap = ws.capacity if table else 0
         for _ in range(6):
             buf = ws.ensure(size(ck_capacity, table_cap))
             rc = call(buf, ck_capacity, table_cap, stream.cuda_stream)
@@ -136,7 +137,7 @@ def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
                 ws.capacity = table_cap
                 return
             ck_capacity = max(ck_capacity, int(st.checkpoints_needed * 1.25) + 1024)
-            if table_cap:
+            if table:
                 table_cap = max(table_cap, int(st.pairs_needed))
             if ck_capacity > 2**31 - 1:
                 raise MemoryError("too many walk checkpoints for one call")
@@ -645,7 +646,6 @@ def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames,
     elem = 4 if out.dtype == torch.float32 else 8
     lib = _native.lib()
     fn = lib.cbc_accumulate_lines_3d_f32 if elem == 4 else lib.cbc_accumulate_lines_3d_f64
-    cap = 0          # the mixed pairs build each term's buffer in shared memory
 
     def check(st):
         if st.has(_native.CBC_ERR_INDEX):
@@ -659,7 +659,7 @@ def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames,
               tm.element_size(), fr.data_ptr(), fr.element_size(), n_terms, max_val, kernel,
               in_ov, out_ov, buf.data_ptr(), buf.numel(), ck, t, stream),
           lambda ck, t: lib.cbc_accumulate_lines_3d_workspace_size(n_lines, n_terms, ck, t, elem),
-          dev, 'accumulate3d', F, n_lines, cap, check)
+          dev, 'accumulate3d', F, n_lines, in_ov != out_ov, check)
     if work is not out:
         out.copy_(work)
     return out

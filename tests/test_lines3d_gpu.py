@@ -84,6 +84,36 @@ def test_accumulate3d_random(cuda, mode, kernel):
         np.testing.assert_allclose(got, ref, **_tol(np.float32, 1.5))
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("mode", [('max', 'sum'), ('sum', 'max')])
+def test_accumulate3d_mixed_term_sizes(cuda, dtype, mode):
+    """terms of 1 to 500 lines in one call: the small ones in shared memory (in one or
+    several partitions), the largest through the workspace table, whose capacity the
+    first call names and the host retries with"""
+    from cbclib_v2_gb300 import ndimage
+    F, D, H, W = 2, 24, 28, 30
+    sizes = [1, 3, 20, 500, 2, 60]
+    rng = np.random.default_rng(31)
+    terms = np.repeat(np.arange(len(sizes)), sizes)
+    n = terms.size
+    centre = rng.random((len(sizes), 3)) * [W, H, D]
+    p0 = centre[terms] + rng.normal(scale=5, size=(n, 3))
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    p1 = p0 + v * rng.uniform(4, 25, n)[:, None]
+    lines = np.concatenate([p0, p1, rng.uniform(0.7, 2.5, (n, 1))], axis=1).astype(dtype)
+    perm = rng.permutation(n)
+    lines, terms = lines[perm], terms[perm]
+    frames = rng.integers(0, F, len(sizes))
+    ref = np.zeros((F, D, H, W), dtype)
+    oracle.accumulate_lines(ref, lines, terms, frames, 1.5, 'gaussian', *mode)
+    out = torch.zeros((F, D, H, W), dtype=torch.from_numpy(ref).dtype, device='cuda')
+    accumulate_lines(out, torch.from_numpy(lines).cuda(), terms, frames, 1.5, 'gaussian', *mode)
+    np.testing.assert_allclose(out.cpu().numpy(), ref, **_tol(dtype, 1.5))
+    ws = next(w for k, w in ndimage._workspaces.items() if k[0] == 'accumulate3d')
+    assert ws.capacity > 0                      # the largest terms went through the table
+
+
 def test_accumulate3d_golden(cuda, golden):
     """the reference rotomap's form: gaussian, max within terms, sum across terms"""
     cases = {k: c for k, c in golden.items() if c['kind'] == 'accumulate' and c['ndim'] == 3}
