@@ -340,11 +340,14 @@ CBC_API int cbc_adam_step_f32(float *params, const float *grad, float *exp_avg,
  * CBC_ERR_INDEX (idx_min / idx_max hold the frames' range), a term outside
  * [0, n_terms) sets CBC_ERR_TERM (bad_line: the first such line).
  *
- * The mixed pairs (sum in / max out, max in / sum out) keep per (term, pixel) values
- * in a hash table of `table_capacity` entries (a power of two; 12 or 16 bytes each)
- * in the workspace, about twice the number of (term, pixel) pairs drawn.  A full
- * table sets CBC_ERR_CAPACITY with pairs_needed = a capacity to retry with; so does a
- * checkpoint overflow, with checkpoints_needed.  The equal pairs use no table. */
+ * The mixed pairs (sum in / max out, max in / sum out) build each term's buffer in
+ * shared memory, in up to eight partitions of its pixels.  Terms whose pixel estimate
+ * needs more partitions keep their (term, pixel) values in a hash table of
+ * `table_capacity` entries (0 or a power of two; 12 or 16 bytes each) in the
+ * workspace; the call requires twice their estimated pairs and otherwise sets
+ * CBC_ERR_CAPACITY with pairs_needed = the capacity to retry with, drawing nothing.
+ * Calls without such terms need no table (table_capacity 0).  A checkpoint overflow
+ * sets CBC_ERR_CAPACITY with checkpoints_needed.  The equal pairs use no table. */
 CBC_API size_t cbc_accumulate_lines_workspace_size(int64_t n_lines, int64_t n_terms,
                                                    int64_t checkpoint_capacity,
                                                    int64_t table_capacity, int32_t elem_bytes);
@@ -394,10 +397,10 @@ CBC_API int cbc_draw_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, 
                                   void *stream);
 
 /* accumulate_lines for 3-D lines into volumes (N = 3 of bresenham.cpp:151-259;
- * cuda_draw_lines.cu:1034-1042), with the arguments and status of
- * cbc_accumulate_lines_f32 plus the volume depth.  The mixed pairs build each term's
- * buffer in shared memory (in partitions of its voxels when it is large) and need no
- * table: table_capacity is not used (any value >= 0). */
+ * cuda_draw_lines.cu:1034-1042), with the arguments, status and table_capacity rule
+ * of cbc_accumulate_lines_f32 plus the volume depth (eight partitions of a 8192-voxel
+ * shared-memory table per term before a term goes to the workspace table).  The
+ * checkpoint capacity counts one checkpoint per long-axis column of each line. */
 CBC_API size_t cbc_accumulate_lines_3d_workspace_size(int64_t n_lines, int64_t n_terms,
                                                       int64_t checkpoint_capacity,
                                                       int64_t table_capacity,
