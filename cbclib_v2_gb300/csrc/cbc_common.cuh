@@ -146,9 +146,14 @@ template <> struct Ar<double> {
     static __device__ __forceinline__ double sqrt(double a) { return __dsqrt_rn(a); }
     static __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
     static __device__ __forceinline__ double from_int(int v) { return (double)v; }
+    /* the quotients below: from the correctly rounded reciprocal (cbc_ddiv) when len
+     * and ww lie in its range, otherwise the IEEE division; the same double either way */
+    static __device__ __forceinline__ double qdiv(double a, double b, double rb, int fast) {
+        return fast ? cbc_ddiv(a, b, rb) : __ddiv_rn(a, b);
+    }
     /* normal_error: T accumulator fed with pow(b, 2) = fl(b * b) (bresenham.hpp:284-289) */
     static __device__ __forceinline__ double nterm(double ne, const SlotParams<double> &p) {
-        double b = __ddiv_rn(ne, p.len);
+        double b = qdiv(ne, p.len, p.rlen, p.fast);
         return __dmul_rn(b, b);
     }
     /* error(): fl(fl(fl(a * a) + nf) / ww) (bresenham.hpp:291-296) */
@@ -157,11 +162,11 @@ template <> struct Ar<double> {
         double m1 = -te, m2 = __dsub_rn(te, p.len2);
         double ta = (m1 < m2) ? m2 : m1;
         if (ta < 0.0) ta = 0.0;
-        double a = __ddiv_rn(ta, p.len);
-        return __ddiv_rn(__dadd_rn(__dmul_rn(a, a), nf), p.ww);
+        double a = qdiv(ta, p.len, p.rlen, p.fast);
+        return qdiv(__dadd_rn(__dmul_rn(a, a), nf), p.ww, p.rww, p.fast);
     }
     static __device__ __forceinline__ double error_inside(double nf, const SlotParams<double> &p) {
-        return __ddiv_rn(nf, p.ww);
+        return qdiv(nf, p.ww, p.rww, p.fast);
     }
     template <int K>
     static __device__ __forceinline__ double profile(double x) { return cbc_profile_f64(K, x); }
@@ -169,7 +174,9 @@ template <> struct Ar<double> {
     static __device__ __forceinline__ double profile_tab(double x, const float *) {
         return cbc_profile_f64(K, x);
     }
-    static __device__ __forceinline__ bool fast_range(double) { return false; }
+    static __device__ __forceinline__ bool fast_range(double v) {
+        return v >= CBC_DDIV_LO && v <= CBC_DDIV_HI;
+    }
 };
 
 /* ---- line preparation ---------------------------------------------------------- */

@@ -164,11 +164,11 @@ __device__ __forceinline__ T normal_error(const Rec3<T> &r, const It3<T> &it)
                    ? cbc_normal_error3_r(it.ne[0], it.ne[1], it.ne[2], r.len, r.rlen)
                    : cbc_normal_error3(it.ne[0], it.ne[1], it.ne[2], r.len);
     } else {
-        using A = Ar<T>;
+        const int fast = (r.flags & kFastDiv) ? 1 : 0;
         T err = T(0);
         #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const double b = (double)A::div(it.ne[k], r.len);
+            const double b = Ar<double>::qdiv(it.ne[k], r.len, r.rlen, fast);
             err = (T)__dadd_rn((double)err, __dmul_rn(b, b));
         }
         return err;
@@ -185,12 +185,13 @@ __device__ __forceinline__ T error(const Rec3<T> &r, const It3<T> &it, T nf)
                    : cbc_pixel_error(it.te, nf, r.len, r.len2, r.ww);
     } else {
         using A = Ar<T>;
+        const int fast = (r.flags & kFastDiv) ? 1 : 0;
         const T m1 = -it.te, m2 = A::sub(it.te, r.len2);
         T ta = m1 < m2 ? m2 : m1;
         ta = ta < T(0) ? T(0) : ta;
-        const double a = (double)A::div(ta, r.len);
+        const double a = Ar<double>::qdiv(ta, r.len, r.rlen, fast);
         const double e = __dadd_rn(__dmul_rn(a, a), (double)nf);
-        return (T)__ddiv_rn(e, (double)r.ww);
+        return (T)Ar<double>::qdiv(e, r.ww, r.rww, fast);
     }
 }
 

@@ -80,3 +80,8 @@ void exact_normal_error3_batch(const float *n0, const float *n1, const float *n2
         }
     }
 }
+
+void exact_ddiv_batch(const double *a, const double *b, double *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++) out[i] = cbc_ddiv(a[i], b[i], 1.0 / b[i]);
+}

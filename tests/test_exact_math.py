@@ -26,6 +26,7 @@ def exact(tmp_path_factory):
     lib.exact_pixel_error_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_pixel_error_r_batch.argtypes = [P] * 5 + [ctypes.c_int64]
     lib.exact_div_batch.argtypes = [P] * 3 + [ctypes.c_int64]
+    lib.exact_ddiv_batch.argtypes = [P] * 3 + [ctypes.c_int64]
     lib.exact_normal_error3_batch.argtypes = [P] * 5 + [ctypes.c_int64, ctypes.c_int]
     lib.exact_take_slow_count.restype = ctypes.c_longlong
     return lib
@@ -107,6 +108,28 @@ def test_reciprocal_division(exact):
     want = a / b
     same = (got == want) | (np.isnan(got) & np.isnan(want))
     assert same.all()
+
+
+def test_reciprocal_division_double(exact):
+    """the double form: the IEEE quotient for b in [2^-400, 2^400], including quotients
+    next to rounding ties (a = b * q + a tiny remainder)"""
+    rng = np.random.default_rng(18)
+    n = 2_000_000
+    ea = rng.integers(-420, 420, n).astype(np.float64)
+    eb = rng.integers(-399, 399, n).astype(np.float64)
+    a = rng.uniform(1, 2, n) * 2.0 ** ea * rng.choice([-1, 1], n)
+    b = rng.uniform(1, 2, n) * 2.0 ** eb
+    a[:100] = 0.0
+    # near ties: a = b * (q + half an ulp of q), rounded
+    m = n // 4
+    q = rng.uniform(1, 2, m)
+    b[-m:] = rng.uniform(1, 2, m) * 2.0 ** rng.integers(-50, 50, m)
+    a[-m:] = b[-m:] * (q + np.spacing(q) / 2)
+    got = np.empty(n)
+    exact.exact_ddiv_batch(_p(a), _p(b), _p(got), n)
+    with np.errstate(over='ignore', under='ignore'):
+        want = a / b
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
 
 
 @pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'parabolic'])
