@@ -436,16 +436,13 @@ __device__ __forceinline__ It3<T> collapse(const Rec3<T> &r, const It3<T> &src, 
     return it;
 }
 
-/* quadrant q of a column of draw_line_3d (bresenham.hpp:404-425): the 2-D walk over the
- * short-axis plane in the quadrant's directions and the 1-D spans from each of its
- * voxels; false when the walk ran past its bound (CBC_ERR_RANGE set) */
-template <typename T, class EM>
-__device__ __forceinline__ bool draw_quadrant(const Rec3<T> &r, const It3<T> &it, int q,
-                                              const Vol &v, long long fbase, int line,
-                                              const EM &emit, DevStatus *st)
+/* the start of quadrant q's 2-D walk over the short-axis plane (bresenham.hpp:409-412):
+ * the column's iterator without its long axis, flipped on the quadrant's axes, moved
+ * one step */
+template <typename T>
+__device__ __forceinline__ It3<T> quadrant_start(const Rec3<T> &r, const It3<T> &it, int q)
 {
     const int ax = r.axis, ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
-    long long guard = 0;
     It3<T> ixy = it;
     put3(ixy.step, ax, 0);
     if (q & 1) put3(ixy.step, ax1, -at3(ixy.step, ax1));
@@ -453,36 +450,68 @@ __device__ __forceinline__ bool draw_quadrant(const Rec3<T> &r, const It3<T> &it
     update(r, ixy);
     increment_at(r, ixy, ((q & 1) ^ (q >> 1)) == 0 ? ax1 : ax2);      /* move */
     update(r, ixy);
-    for (T nxy; (nxy = normal_error(r, ixy)) < r.ww; advance(r, ixy)) {
-        visit(r, ixy, nxy, v, fbase, line, emit);
-        for (int j = 1; j < 3; j++) {
-            const int aj = (ax + j) % 3;
-            if (!at3(ixy.next, aj)) continue;
-            It3<T> ix = collapse(r, ixy, aj);
-            advance(r, ix);
-            for (T nx; (nx = normal_error(r, ix)) < r.ww; advance(r, ix)) {
-                visit(r, ix, nx, v, fbase, line, emit);
-                if (++guard > 4LL * CBC_MAX_WALK) break;
-            }
-        }
-        if (++guard > 4LL * CBC_MAX_WALK) {
-            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
-            return false;
-        }
-    }
-    return true;
+    return ixy;
 }
 
 /* quadrants [q0, q1) of a column of draw_line_3d (bresenham.hpp:392-428), with the
- * centre voxel when q0 is 0 */
+ * centre voxel when q0 is 0.  The reference's nested loops (the quadrant's 2-D walk
+ * while normal_error < width^2, from each of its positions a 1-D span along each
+ * short axis with a next step) are run as one loop that looks at one position per
+ * iteration: the centre, a 2-D walk position (mode 0) or a span position (mode 1).
+ * Each iteration evaluates one normal error and makes at most one visit, so the lanes
+ * of a warp, wherever they are in their walks, share the expensive part of the
+ * iteration; the visit order is the reference's. */
 template <typename T, class EM>
 __device__ __forceinline__ void draw_quadrants(const Rec3<T> &r, const It3<T> &it, int q0,
                                                int q1, const Vol &v, long long fbase, int line,
                                                const EM &emit, DevStatus *st)
 {
-    if (q0 == 0) visit(r, it, normal_error(r, it), v, fbase, line, emit);
-    for (int q = q0; q < q1; q++)
-        if (!draw_quadrant(r, it, q, v, fbase, line, emit, st)) return;
+    const int ax = r.axis;
+    int q = q0, mode = 0, j = 0;
+    bool centre = q0 == 0;
+    It3<T> ixy = quadrant_start(r, it, q);
+    It3<T> ix = ixy;
+    long long guard = 0;
+    for (;;) {
+        const It3<T> cur = centre ? it : (mode ? ix : ixy);
+        const T nf = normal_error(r, cur);
+        const bool in = centre || nf < r.ww;
+        if (in) visit(r, cur, nf, v, fbase, line, emit);
+        /* the transition: which iterator steps next (one advance site for both) */
+        bool step = true;
+        if (centre) {
+            centre = false;                      /* then quadrant q0's first position */
+            step = false;
+        } else if (mode == 0 || !in) {
+            if (mode == 0 && !in) {              /* the quadrant's 2-D walk has ended */
+                if (++q >= q1) return;
+                ixy = quadrant_start(r, it, q);
+                step = false;
+            } else {
+                j = mode == 0 ? 1 : j + 1;       /* a new position, or a span ended */
+                /* the next span from the current 2-D position, else its next position */
+                mode = 0;
+                for (; j < 3; j++) {
+                    const int aj = (ax + j) % 3;
+                    if (at3(ixy.next, aj)) {
+                        ix = collapse(r, ixy, aj);
+                        mode = 1;
+                        break;
+                    }
+                }
+            }
+        }
+        if (step) {
+            It3<T> nxt = mode ? ix : ixy;
+            advance(r, nxt);
+            if (mode) ix = nxt;
+            else ixy = nxt;
+        }
+        if (++guard > 8LL * CBC_MAX_WALK) {
+            atomicOr(&st->flags, 1 << CBC_ERR_RANGE);
+            return;
+        }
+    }
 }
 
 /* the iterator at a column from the column's checkpoint */
