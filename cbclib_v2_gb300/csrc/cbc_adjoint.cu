@@ -193,15 +193,45 @@ struct BackwardAct {
         p.g = grad_out ? grad_out[at] : T(2) * (image[at] - target[at]);
         return p;
     }
+    /* this lane's term of the current drain batch, added in batch_end */
+    T pv[5];
+    int pslot = -1;
     __device__ __forceinline__ void pixel(const SlotTable<T> &S, int slot, int px, int py, T, T,
                                           T, const Pre &p) {
         const T g = p.g;
         if (g == T(0)) return;
-        T v[5];
-        pixel_term<T, K>(coef[slot], g, (T)px, (T)py, v);
+        pixel_term<T, K>(coef[slot], g, (T)px, (T)py, pv);
+        pslot = slot;
+    }
+    /* the batch's terms into the per-slot sums: lanes holding the same slot (the lanes
+     * of one drain batch often do) are summed by shuffles into their lowest lane, which
+     * alone adds to the slot, so the sums need no shared-memory atomics */
+    __device__ __forceinline__ void batch_end(int lane) {
+        const int key = pslot;
+        if (__ballot_sync(0xffffffffu, key >= 0) == 0u) return;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        const int most = __reduce_max_sync(0xffffffffu, key >= 0 ? __popc(peers) : 0);
+        T s[5];
         #pragma unroll
-        for (int k = 0; k < 5; k++)
-            if (v[k] != T(0)) atomicAdd(&acc[slot][k], v[k]);
+        for (int k = 0; k < 5; k++) s[k] = pv[k];
+        unsigned rest = peers & (peers - 1u);            /* the group without its leader */
+        for (int r = 1; r < most; r++) {
+            const int src = rest ? __ffs(rest) - 1 : lane;
+            const bool take = lane == leader && rest != 0u;
+            #pragma unroll
+            for (int k = 0; k < 5; k++) {
+                const T o = __shfl_sync(0xffffffffu, pv[k], src);
+                if (take) s[k] += o;
+            }
+            rest &= rest - 1u;
+        }
+        if (key >= 0 && lane == leader) {
+            #pragma unroll
+            for (int k = 0; k < 5; k++)
+                if (s[k] != T(0)) acc[key][k] += s[k];
+        }
+        pslot = -1;
     }
 };
 

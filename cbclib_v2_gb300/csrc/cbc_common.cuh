@@ -866,6 +866,12 @@ template <class A, class = void> struct FiltersLines : std::false_type {};
 template <class A>
 struct FiltersLines<A, std::void_t<decltype(&A::keep_line)>> : std::true_type {};
 
+/* actions that combine a drain batch's results across the warp define batch_end(lane),
+ * called by all 32 lanes after every batch */
+template <class A, class = void> struct EndsBatches : std::false_type {};
+template <class A>
+struct EndsBatches<A, std::void_t<decltype(&A::batch_end)>> : std::true_type {};
+
 template <typename T, class Act>
 __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
 {
@@ -952,6 +958,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                     act.pixel(S, slot, v.x, v.y, T(0), v.te, v.ne, pre);
                 }
             }
+            if constexpr (EndsBatches<Act>::value) act.batch_end(lane);
             head += n;
             __syncwarp();
         }
