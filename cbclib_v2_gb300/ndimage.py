@@ -106,12 +106,22 @@ def _volumes_of(out: torch.Tensor):
     return math.prod(int(s) for s in out.shape[:-3]), D, H, W
 
 
+def _columns3(ln: torch.Tensor, extent: int) -> int:
+    """An upper estimate of the long-axis columns of (N, 7) 3-D lines in volumes whose
+    largest side is ``extent``: the 3-D renders keep one walk checkpoint per column."""
+    span = (ln[:, 3:6] - ln[:, 0:3]).abs().amax(dim=1) + 2 * ln[:, 6].clamp(min=0).ceil() + 3
+    span = torch.nan_to_num(span, nan=0.0, posinf=float(extent), neginf=0.0)
+    return int(span.clamp(max=float(extent)).sum().item())
+
+
 def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
-          table: bool = False, on_status=None) -> None:
+          table: bool = False, on_status=None, columns=None) -> None:
     """Run a 3-D library call ``call(buf, ck_capacity, table_capacity, stream)`` with
     this thread's workspace, raise the status' errors and retry with more room when the
     call reports that its checkpoints or (``table``: mixed-overlap accumulate) its
-    workspace table did not fit."""
+    workspace table did not fit.  ``columns()`` estimates the checkpoints the call
+    needs; it runs (one synchronisation) only when the workspace's are fewer than the
+    default."""
     lib = _native.lib()
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev)
@@ -119,6 +129,8 @@ def _run3(call, size, dev: torch.device, kind: str, n_frames: int, n_lines: int,
         with _ws_lock:
             ws = _workspaces.setdefault(key, Workspace(dev))
         ck_capacity = max(ws.ck_capacity, 16 * n_lines + 1024)
+        if columns is not None and ws.ck_capacity < ck_capacity:
+            ck_capacity = max(ck_capacity, int(columns() * 1.25) + 1024)
         table_cap = ws.capacity if table else 0
         for _ in range(6):
             buf = ws.ensure(size(ck_capacity, table_cap))
@@ -160,7 +172,7 @@ def _draw_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, idxs, max_val: float
               None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
               max_val, kernel, overlap, buf.data_ptr(), buf.numel(), ck, stream),
           lambda ck, _t: lib.cbc_draw_lines_3d_workspace_size(n_lines, ck, elem),
-          out.device, 'draw3d', F, n_lines)
+          out.device, 'draw3d', F, n_lines, columns=lambda: _columns3(ln, max(D, H, W)))
     if work is not out:
         out.copy_(work)
     return out
@@ -659,7 +671,8 @@ def _accumulate_lines3d_cuda(out: torch.Tensor, ln: torch.Tensor, terms, frames,
               tm.element_size(), fr.data_ptr(), fr.element_size(), n_terms, max_val, kernel,
               in_ov, out_ov, buf.data_ptr(), buf.numel(), ck, t, stream),
           lambda ck, t: lib.cbc_accumulate_lines_3d_workspace_size(n_lines, n_terms, ck, t, elem),
-          dev, 'accumulate3d', F, n_lines, in_ov != out_ov, check)
+          dev, 'accumulate3d', F, n_lines, in_ov != out_ov, check,
+          columns=lambda: _columns3(ln, max(D, H, W)))
     if work is not out:
         out.copy_(work)
     return out
