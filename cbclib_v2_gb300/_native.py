@@ -61,6 +61,7 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_squared_loss_backward_f64', 'cbc_draw_lines_max_winner_f32',
            'cbc_draw_lines_backward_ex_f32', 'cbc_draw_lines_backward_ex_f64',
            'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32',
+           'cbc_squared_loss_step_sum_f32',
            'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status',
            'cbc_adam_step_f32', 'cbc_draw_lines_host_f32', 'cbc_draw_lines_host_f64')
 
@@ -134,6 +135,10 @@ def _declare(lib):
     lib.cbc_squared_loss_step_f32.argtypes = [p, i64, i64, i64, p, i64, p, i32, ctypes.c_float,
                                               i32, p, p, p, p, ctypes.c_size_t, i64, i64, p]
     lib.cbc_squared_loss_step_f32.restype = ctypes.c_int
+    lib.cbc_squared_loss_step_sum_f32.argtypes = [p, p, i64, i64, i64, p, i64, p, i32,
+                                                  ctypes.c_float, i32, p, p, p, ctypes.c_size_t,
+                                                  i64, i64, p]
+    lib.cbc_squared_loss_step_sum_f32.restype = ctypes.c_int
     for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
         f = getattr(lib, 'cbc_draw_lines_host_' + sfx)
         f.argtypes = [p, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, i32, p,

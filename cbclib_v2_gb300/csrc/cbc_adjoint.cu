@@ -1027,6 +1027,109 @@ int loss_step_impl(const float *target, long long n_frames, long long H, long lo
     return CBC_OK;
 }
 
+/* sum over the frames of (image - target)^2 into *loss (zeroed before) */
+__global__ void __launch_bounds__(256)
+sq_diff_kernel(const float *__restrict__ image, const float *__restrict__ target, long long n,
+               double *loss)
+{
+    __shared__ double warp_sums[8];
+    double acc = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double d = (double)image[i] - (double)target[i];
+        acc += d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < 8; w++) b += warp_sums[w];
+        atomicAdd(loss, b);
+    }
+}
+
+/* the sum-overlap squared-loss step: the forward into `image` (zeroed first) with the
+ * lines strategy, then the adjoint walks over the forward's own line records and walk
+ * checkpoints (no second prep), then the (N, 5) gradient and, if asked, the loss */
+int sum_loss_step_impl(const float *target, float *image, long long n_frames, long long H,
+                       long long W, const float *lines, long long n_lines, const void *idxs,
+                       int idx_bytes, float max_val, int kernel, float *grad_lines,
+                       double *loss, void *workspace, size_t ws_bytes, long long capacity,
+                       long long ck_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || H < 0 || W < 0 || n_lines < 0 || capacity < 0 || ck_capacity < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    const long long px = n_frames * H * W;
+    if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (px > 0 && (!target || !image)) return fail(CBC_ERR_INVALID, "null target or image");
+    StepLayout L;
+    if (!step_layout(n_frames, H, W, n_lines, capacity, ck_capacity, L))
+        return fail(CBC_ERR_INVALID, "invalid sizes");
+    if (!workspace || ws_bytes < L.total)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(L.total) + ")");
+    cbc_tuning t{};
+    t.strategy = CBC_STRATEGY_LINES;
+    size_t recs_off = 0, cks_off = 0;
+    if (!draw_workspace_parts(n_frames, H, W, n_lines, capacity, ck_capacity, 4, &t, &recs_off,
+                              &cks_off))
+        return fail(CBC_ERR_INVALID, "invalid sizes");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    if (px > 0) e = cudaMemsetAsync(image, 0, sizeof(float) * (size_t)px, s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    int rc = cbc_draw_lines_f32(image, n_frames, H, W, lines, n_lines, idxs, idx_bytes, max_val,
+                                kernel, CBC_SUM, workspace, L.draw, capacity, ck_capacity, &t,
+                                stream);
+    if (rc != CBC_OK) return rc;
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws);      /* the forward's status block */
+    double *gacc = reinterpret_cast<double *>(ws + L.gacc);
+    e = cudaMemsetAsync(gacc, 0, sizeof(double) * (5 * (size_t)n_lines + 1), s);
+    /* the forward's render consumed the work counter; the adjoint walks start it again */
+    if (e == cudaSuccess) e = cudaMemsetAsync(&st->work, 0, sizeof(st->work), s);
+    if (e == cudaSuccess && loss) e = cudaMemsetAsync(loss, 0, sizeof(double), s);
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines > 0 && px > 0) {
+        AdjArgs<float> aa{};
+        aa.d.recs = reinterpret_cast<const LineRec<float> *>(ws + recs_off);
+        aa.d.cks = reinterpret_cast<const Checkpoint<float> *>(ws + cks_off);
+        aa.d.H = (int)H;
+        aa.d.W = (int)W;
+        aa.d.st = st;
+        aa.d.work = &st->work;
+        aa.image = image;
+        aa.target = target;
+        aa.gacc = gacc;
+        aa.max_val = max_val;
+        switch (kernel) {
+        case CBC_BIWEIGHT:    e = launch_walks<float, CBC_BIWEIGHT>(aa, CBC_SUM, s); break;
+        case CBC_GAUSSIAN:    e = launch_walks<float, CBC_GAUSSIAN>(aa, CBC_SUM, s); break;
+        case CBC_PARABOLIC:   e = launch_walks<float, CBC_PARABOLIC>(aa, CBC_SUM, s); break;
+        case CBC_RECTANGULAR: e = launch_walks<float, CBC_RECTANGULAR>(aa, CBC_SUM, s); break;
+        default:              e = launch_walks<float, CBC_TRIANGULAR>(aa, CBC_SUM, s); break;
+        }
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const long long n5 = 5 * n_lines;
+    if (n5 > 0) {
+        finalize_kernel<float><<<(unsigned)((n5 + 255) / 256), 256, 0, s>>>(
+            gacc, grad_lines, n5, nullptr, 0, nullptr);
+        note_launches(1);
+    }
+    if (loss && px > 0) {
+        long long blocks = (px + 255) / 256;
+        if (blocks > 4096) blocks = 4096;
+        sq_diff_kernel<<<(unsigned)blocks, 256, 0, s>>>(image, target, px, loss);
+        note_launches(1);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
 /* one Adam step on the (N, 5) line parameters with the width clamp:
  * m = m + (1 - b1)(g - m), v = b2 v + (1 - b2) g^2,
  * p -= (lr / (1 - b1^t)) m / (sqrt(v) / sqrt(1 - b2^t) + eps), widths >= min_width */
@@ -1050,6 +1153,19 @@ adam_kernel(float *__restrict__ p, const float *__restrict__ g, float *__restric
 }  // namespace cbc
 
 extern "C" {
+
+int cbc_squared_loss_step_sum_f32(const float *target, float *image, int64_t n_frames,
+                                  int64_t height, int64_t width, const float *lines,
+                                  int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                  float max_val, int32_t kernel, float *grad_lines,
+                                  double *loss, void *workspace, size_t workspace_bytes,
+                                  int64_t pair_capacity, int64_t checkpoint_capacity,
+                                  void *stream)
+{
+    return cbc::sum_loss_step_impl(target, image, n_frames, height, width, lines, n_lines, idxs,
+                                   idx_bytes, max_val, kernel, grad_lines, loss, workspace,
+                                   workspace_bytes, pair_capacity, checkpoint_capacity, stream);
+}
 
 int cbc_adam_step_f32(float *params, const float *grad, float *exp_avg, float *exp_avg_sq,
                       int64_t n_lines, int64_t step, float lr, float beta1, float beta2,

@@ -1126,6 +1126,11 @@ unsigned resident_grid(F kernel, int threads)
 
 /* host-side error reporting, defined in cbc_draw_lines.cu */
 int fail(int code, const std::string &msg);
+/* offsets of the line records and walk checkpoints in a draw_lines workspace laid out
+ * for these sizes and tuning (false for an invalid tuning), defined in cbc_draw_lines.cu */
+bool draw_workspace_parts(long long n_frames, long long H, long long W, long long n_lines,
+                          long long capacity, long long ck_capacity, size_t elem,
+                          const cbc_tuning *tuning, size_t *recs, size_t *cks);
 void clear_error();
 /* adds n to the library's kernel-launch counter (reported by cbc_profile_read) */
 void note_launches(int n);

@@ -926,6 +926,22 @@ int draw_lines_host_impl(T *host_out, long long n_frames, long long H, long long
     return CBC_OK;
 }
 
+bool draw_workspace_parts(long long n_frames, long long H, long long W, long long n_lines,
+                          long long capacity, long long ck_capacity, size_t elem,
+                          const cbc_tuning *tuning, size_t *recs, size_t *cks)
+{
+    Resolved t;
+    std::string why;
+    if (!resolve_tuning(tuning, t, why)) return false;
+    const Layout L = make_layout(n_frames, H, W, n_lines, capacity, ck_capacity,
+                                 elem == 4 ? sizeof(LineRec<float>) : sizeof(LineRec<double>),
+                                 elem == 4 ? sizeof(Checkpoint<float>) : sizeof(Checkpoint<double>),
+                                 t);
+    *recs = L.recs;
+    *cks = L.cks;
+    return true;
+}
+
 }  // namespace cbc
 
 extern "C" {

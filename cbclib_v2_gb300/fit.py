@@ -75,6 +75,41 @@ def _packed_loss_step(target: torch.Tensor, lines, idxs, max_val: float, kernel:
     return grad
 
 
+def _sum_loss_step(image: torch.Tensor, target: torch.Tensor, lines, idxs, max_val: float,
+                   kernel: str, loss: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """cbc_squared_loss_step_sum_f32: the sum-overlap forward into ``image`` and the
+    gradient of sum((image - target)^2), the adjoint walking the forward's own
+    checkpoints, in one library call; ``loss`` (a float64 CUDA scalar, or None)
+    receives the loss."""
+    k, _ = ndimage._check_names(kernel, 'sum')
+    dev = target.device
+    F, H, W = ndimage._frames_of(target)
+    if tuple(image.shape) != tuple(target.shape) or not image.is_contiguous():
+        raise ValueError("image must be a contiguous tensor of the target's shape")
+    ln = ndimage._as_device_lines(lines, dev, torch.float32)
+    if ln.shape[1] != 5:
+        raise ValueError("the fused loss step takes 2-D lines (N, 5)")
+    n = ln.shape[0]
+    ix = ndimage._as_device_idxs(idxs, n, dev)
+    if ix is None and n and F != 1 and F != n:
+        raise ValueError(f"idxs has an incompatible size ({n} != {F})")
+    tg = target.contiguous()
+    grad = torch.empty((n, 5), dtype=torch.float32, device=dev)
+    lib = _native.lib()
+    loss_ptr = None if loss is None else loss.data_ptr()
+
+    def call(buf, capacity, ck_capacity, tref, stream):
+        return lib.cbc_squared_loss_step_sum_f32(
+            tg.data_ptr(), image.data_ptr(), F, H, W, ln.data_ptr(), n,
+            None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+            max_val, k, grad.data_ptr(), loss_ptr, buf.data_ptr(), buf.numel(), capacity,
+            ck_capacity, stream)
+
+    ndimage._run_with_workspace(call, dev, F, H, W, n, 4, None,
+                                size_fn=lib.cbc_squared_loss_step_workspace_size)
+    return grad
+
+
 class _PackedSteps:
     """The fused loss steps of one fit: the first step runs through the checking
     path (which sizes the workspace), later steps enqueue the library call and an
@@ -153,6 +188,9 @@ def squared_loss_step(image: Optional[torch.Tensor], target: torch.Tensor, lines
         winner = ndimage.draw_lines_max_winner(image, lines, idxs, max_val, kernel, winner)
         return squared_loss_backward(image, target, lines, idxs, max_val, kernel, overlap,
                                      winner=winner, winner_known=True)
+    if overlap == 'sum' and image.dtype == torch.float32 and target.dtype == torch.float32 \
+            and image.is_cuda and image.is_contiguous():
+        return _sum_loss_step(image, target, lines, idxs, max_val, kernel)
     image.zero_()
     ndimage.draw_lines(image, lines, idxs, max_val, kernel, overlap)
     return squared_loss_backward(image, target, lines, idxs, max_val, kernel, overlap,

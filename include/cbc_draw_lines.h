@@ -291,6 +291,21 @@ CBC_API int cbc_squared_loss_step_f32(const float *target, int64_t n_frames, int
                                       size_t workspace_bytes, int64_t pair_capacity,
                                       int64_t checkpoint_capacity, void *stream);
 
+/* The same step for float32 sum overlap: `image` (n_frames * height * width device
+ * floats) is zeroed and receives draw(lines); the adjoint then walks the forward's own
+ * line records and walk checkpoints (no second preparation) and writes the gradient of
+ * L = sum((image - target)^2) into grad_lines.  loss (device double, may be NULL)
+ * receives L.  Workspace size: cbc_squared_loss_step_workspace_size; its start is the
+ * forward's, so cbc_read_status on it reports the forward's errors and capacity
+ * needs.  No counterpart in the reference (new). */
+CBC_API int cbc_squared_loss_step_sum_f32(const float *target, float *image, int64_t n_frames,
+                                          int64_t height, int64_t width, const float *lines,
+                                          int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                          float max_val, int32_t kernel, float *grad_lines,
+                                          double *loss, void *workspace,
+                                          size_t workspace_bytes, int64_t pair_capacity,
+                                          int64_t checkpoint_capacity, void *stream);
+
 /* draw_lines into frames in page-locked host memory (cudaHostAlloc, or registered),
  * which the kernels address directly (NVLink-C2C on GB300): the lines are drawn into
  * `scratch` (n_frames * height * width device elements), which must hold the

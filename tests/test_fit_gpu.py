@@ -169,3 +169,35 @@ def test_unchecked_steps_fall_back_when_checkpoints_run_out(cuda, monkeypatch):
     monkeypatch.setattr(fit._PackedSteps, 'first', first)
     again = fit.fit_lines(target, start, idxs, **kw)
     torch.testing.assert_close(again.lines, want.lines, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("kernel", ['biweight', 'gaussian', 'triangular'])
+def test_sum_loss_step_matches_two_calls(cuda, kernel):
+    """cbc_squared_loss_step_sum_f32 (forward, then the adjoint over the forward's own
+    checkpoints) against draw_lines followed by the separate adjoint, with lines long
+    enough for the long-walk list, int64 indices, and the loss it reports"""
+    from cbclib_v2_gb300.autograd import squared_loss_backward
+    rng = np.random.default_rng(12)
+    F, H, W, n = 3, 150, 260, 300
+    p0 = rng.random((n, 2)) * [W, H]
+    v = rng.normal(size=(n, 2))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    p1 = p0 + v * rng.uniform(2, 240, n)[:, None]          # some walks beyond 96 columns
+    lines = torch.from_numpy(np.concatenate([p0, p1, rng.uniform(0.5, 4, (n, 1))], 1)
+                             .astype(np.float32)).cuda()
+    idxs = torch.from_numpy(rng.integers(0, F, n)).cuda()
+    target = torch.rand((F, H, W), device='cuda') * 3
+    image = torch.empty_like(target)
+    loss = torch.zeros((), dtype=torch.float64, device='cuda')
+    g = fit._sum_loss_step(image, target, lines, idxs, 2.0, kernel, loss)
+    ref_img = torch.zeros_like(target)
+    draw_lines(ref_img, lines, idxs, 2.0, kernel, 'sum')
+    ref_g = squared_loss_backward(ref_img, target, lines, idxs, 2.0, kernel, 'sum')
+    torch.testing.assert_close(image, ref_img, rtol=1e-5, atol=1e-5)
+    torch.testing.assert_close(g, ref_g, rtol=1e-4, atol=1e-3)
+    want = ((ref_img.double() - target.double()) ** 2).sum()
+    torch.testing.assert_close(loss, want, rtol=1e-9, atol=1e-6)
+    # no lines: zero frames, the loss of the empty image
+    g0 = fit._sum_loss_step(image, target, lines[:0], idxs[:0], 2.0, kernel, loss)
+    assert g0.shape == (0, 5) and not image.any()
+    torch.testing.assert_close(loss, (target.double() ** 2).sum(), rtol=1e-9, atol=1e-6)
