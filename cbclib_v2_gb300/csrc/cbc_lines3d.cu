@@ -544,7 +544,7 @@ struct Render3Args {
  * collide on the voxels the quadrants share), grid-stride; quadrant 0 also takes the
  * centre voxel */
 template <typename T, int K>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 2)
 render3_kernel(Render3Args<T> a, Emit3<T, K> emit)
 {
     if (a.st->flags & kFatal) return;
