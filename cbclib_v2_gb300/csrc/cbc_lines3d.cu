@@ -210,7 +210,7 @@ __device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
     for (int i = 0; i < 3; i++) r.tau[i] = A::sub(p1[i], p0[i]);
     int ax = 0;
     for (int i = 1; i < 3; i++)
-        if (fabs(r.tau[ax]) < fabs(r.tau[i])) ax = i;
+        if (fabs(at3(r.tau, ax)) < fabs(r.tau[i])) ax = i;
     r.axis = ax;
     T mag = T(0);
     for (int i = 0; i < 3; i++) mag = A::add(mag, A::mul(r.tau[i], r.tau[i]));
@@ -220,7 +220,7 @@ __device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
     if (!(ceilw < T(1e9))) return false;
     T tn[3];
     for (int i = 0; i < 3; i++) tn[i] = A::div(r.tau[i], r.len);
-    const T scale = fabs(A::div(ceilw, tn[ax]));
+    const T scale = fabs(A::div(ceilw, at3(tn, ax)));
     int32_t mpt0[3];
     const T lim = T(1 << 30);
     for (int i = 0; i < 3; i++) {
@@ -231,9 +231,9 @@ __device__ bool build_rec3(const T *ln, Rec3<T> &r, It3<T> &it, bool &too_long)
         mpt0[i] = (int32_t)a;
         r.mpt1[i] = (int32_t)b + r.step[i];
     }
-    long long walk = (long long)r.mpt1[ax] - mpt0[ax];
+    long long walk = (long long)at3(r.mpt1, ax) - at3(mpt0, ax);
     if (walk < 0) walk = -walk;
-    const T span = A::div(A::mul(w, r.len), fabs(r.tau[ax]));
+    const T span = A::div(A::mul(w, r.len), fabs(at3(r.tau, ax)));
     if (walk > CBC_MAX_WALK || !(span < T(CBC_MAX_WALK))) { too_long = true; return false; }
     for (int k = 0; k < 3; k++)
         for (int i = 0; i < 3; i++) r.nrm[k][i] = T(0);
@@ -299,8 +299,8 @@ prep3_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lo
             if (build_rec3(lines + 7 * i, r, it, too_long)) {
                 r.frame = (int32_t)frame;
                 const int ax = r.axis;
-                sa = r.step[ax];
-                const int first = it.cur[ax], last = r.mpt1[ax] - sa;
+                sa = at3(r.step, ax);
+                const int first = at3(it.cur, ax), last = at3(r.mpt1, ax) - sa;
                 lmin = max(min(first, last), 0);
                 lmax = min(max(first, last), v.ext(ax) - 1);
                 if (lmin <= lmax) {
