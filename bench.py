@@ -6,21 +6,30 @@ indices): one step = one draw_lines call over the whole stack.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput in Mlines/s
-(lines, indices and frames already in HBM); `e2e` is the same metric through the
-public API with the frames, lines and indices in pinned host buffers: every step copies
-the lines and indices to the device, and the kernels combine the drawn pixels into the
-host frames in place through their device mapping (only drawn pixels cross the link).  `roofline` is the dominant kernel's achieved HBM bandwidth
-(segments_kernel or render_kernel, whichever strategy the call ran) from CUDA events
-recorded on its stream around every launch in the timed region.  Its byte count is the
-call's contract: draw_lines updates `out` in place, so every output pixel is read and
-written once, plus 24 bytes per line (2*F*H*W*4 + 24*N); `write_once_frac` is the same
-for an output known to be zero, and `sparse_model` counts only the 32-byte sectors that
-hold a drawn pixel (the kernel never touches the others).  `gpu_launches` is the library's own count of
-the kernels it launched in the timed region.  `cpu_baseline`
-times the oracle (C port of the reference CPU rasteriser) on a bounded sample with
-all host threads.  Under torchrun each rank renders its own stack (weak scaling, no
-collective on the data path).  `--impl reference` times the reference CPU algorithm
-(the oracle port; the reference sources are not on the GPU host) instead.
+(lines, indices and frames already in HBM).  `e2e` is the same metric through the
+public API the reference's callers use: NumPy frames, lines and indices in host
+memory; every step copies the lines and indices to the device, and the kernels
+combine the drawn pixels into the host frames in place over NVLink-C2C (only drawn
+pixels cross the link); `e2e_pinned` is the same with page-locked torch tensors.
+`roofline` is the dominant kernel's achieved HBM bandwidth (segments_kernel or
+render_kernel, whichever strategy the call ran) from CUDA events recorded on its
+stream around every launch in the timed region.  Its byte count is the call's
+contract: draw_lines updates `out` in place, so every output pixel is read and written
+once, plus 24 bytes per line (2*F*H*W*4 + 24*N); `write_once_frac` is the same for an
+output known to be zero, `sparse_model` counts only the 32-byte sectors that hold a
+drawn pixel (the kernel never touches the others), and `traffic_frac` is the DRAM
+traffic ncu measured for one launch over the launch's time.  `gpu_launches` is the
+library's own count of the kernels it launched in the timed region.  `clocks` are
+NVML samples (every 2 ms) taken inside the timed region.  `cpu_baseline` times the
+oracle (C port of the reference CPU rasteriser) in a fresh process, on all host
+threads and on one, with `out` zeroed and touched before the clock.  `workloads`
+holds the other benchmark configurations, run after the headline: the
+forward+adjoint iterations on 8 x 1024^2 frames against a finite-difference
+gradient, the ragged 256 x 1024^2 stack by one CUDA-graph replay, and the
+32 x 2167x2070 streak-fit loop.  Under torchrun each rank renders its own stack (weak
+scaling, no collective on the data path), or with --shard the ranks split one stack
+by frames.  `--impl reference` times the reference CPU algorithm (the oracle port;
+the reference sources are not on the GPU host) instead.
 """
 import argparse
 import json
@@ -51,6 +60,15 @@ def parse():
                         'reference arm sizes its per-step sample to finish in about a '
                         'minute unless this is set')
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--headline-only', action='store_true',
+                   help='skip the other configurations after the headline')
+    p.add_argument('--shard', action='store_true',
+                   help='under torchrun: split one stack across the ranks by frames '
+                        '(balanced by line counts) instead of one stack per rank')
+    p.add_argument('--cpu-child', action='store_true', help=argparse.SUPPRESS)
+    p.add_argument('--cpu-threads', type=int, default=1, help=argparse.SUPPRESS)
+    p.add_argument('--repeats', type=int, default=1, help=argparse.SUPPRESS)
+    p.add_argument('--seed', type=int, default=1000, help=argparse.SUPPRESS)
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--workload', default='detector_stack',
                    choices=['detector_stack', 'fit', 'ragged', 'fit_loop', 'rotomap',
@@ -79,32 +97,104 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 100 ms; only the samples taken
-    between begin() and end() (the timed region) are reported."""
+    """SM clock, its maximum, power and clock-event reasons of one GPU, sampled every
+    2 ms through NVML (libnvidia-ml, ctypes) from start() to stop(); only samples
+    taken between begin() and end() (the timed region) are reported.  Falls back to
+    `nvidia-smi -lms 100` when NVML cannot be loaded."""
+    REASONS = {0x4: 'sw_power_cap', 0x8: 'hw_slowdown', 0x20: 'sw_thermal_slowdown',
+               0x40: 'hw_thermal_slowdown', 0x80: 'hw_power_brake_slowdown'}
     FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
               'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
               'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, period_s: float = 0.002):
         self.gpu = gpu
-        self.proc = None
-        self.lines = []
+        self.period = period_s
+        self.samples = []              # (time, sm MHz, max MHz, reason bits)
         self.window = (0.0, float('inf'))
+        self.proc = None
+        self.nvml = None
+        self.handle = None
+        self.stop_flag = threading.Event()
+        self.thread = None
+        self.source = None
+
+    def _nvml_open(self):
+        import ctypes
+        try:
+            nv = ctypes.CDLL('libnvidia-ml.so.1')
+        except OSError:
+            return False
+        if nv.nvmlInit_v2() != 0:
+            return False
+        handle = ctypes.c_void_p()
+        found = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.gpu).uuid)
+            found = nv.nvmlDeviceGetHandleByUUID(('GPU-' + uuid).encode(),
+                                                 ctypes.byref(handle)) == 0
+        except Exception:
+            found = False
+        if not found:
+            found = nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.gpu),
+                                                     ctypes.byref(handle)) == 0
+        if not found:
+            return False
+        self.nvml, self.handle = nv, handle
+        return True
+
+    def _nvml_loop(self):
+        import ctypes
+        nv, h = self.nvml, self.handle
+        sm, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_flag.is_set():
+            ok = (nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and
+                  nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and
+                  nv.nvmlDeviceGetCurrentClocksEventReasons(h, ctypes.byref(rs)) == 0)
+            if ok:
+                self.samples.append((time.perf_counter(), float(sm.value), float(mx.value),
+                                     int(rs.value)))
+            time.sleep(self.period)
 
     def start(self):
         """start sampling and wait (at most 10 s) for the first sample"""
-        try:
-            self.proc = subprocess.Popen(
-                ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
-                 '-lms', '100', '-i', str(self.gpu)], stdout=subprocess.PIPE,
-                stderr=subprocess.DEVNULL, text=True)
-            threading.Thread(target=self._read, daemon=True).start()
-        except (OSError, ValueError):
-            self.proc = None
-            return
+        if self._nvml_open():
+            self.source = 'nvml'
+            self.thread = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.thread.start()
+        else:
+            try:
+                self.proc = subprocess.Popen(
+                    ['nvidia-smi', f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
+                     '-lms', '100', '-i', str(self.gpu)], stdout=subprocess.PIPE,
+                    stderr=subprocess.DEVNULL, text=True)
+                self.source = 'nvidia-smi'
+                threading.Thread(target=self._smi_read, daemon=True).start()
+            except (OSError, ValueError):
+                self.proc = None
+                return
         t_end = time.perf_counter() + 10.0
-        while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
-            time.sleep(0.01)
+        while not self.samples and time.perf_counter() < t_end:
+            if self.proc is not None and self.proc.poll() is not None:
+                break
+            time.sleep(0.005)
+
+    def _smi_read(self):
+        names = {'hw_slowdown': 0x8, 'hw_thermal_slowdown': 0x40, 'sw_thermal_slowdown': 0x20,
+                 'sw_power_cap': 0x4}
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.strip().split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                bits = 0
+                for (n, b), v in zip(names.items(), f[5:9]):
+                    if v.lower().startswith('active'):
+                        bits |= b
+                self.samples.append((time.perf_counter(), float(f[1]), float(f[2]), bits))
+            except ValueError:
+                continue
 
     def begin(self):
         self.window = (time.perf_counter(), float('inf'))
@@ -112,38 +202,30 @@ class ClockSampler:
     def end(self):
         self.window = (self.window[0], time.perf_counter())
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append((time.perf_counter(), line.strip()))
-
     def stop(self):
-        if self.proc is None:
-            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        lo, hi = self.window
-        for t, ln in self.lines:
-            if not lo <= t <= hi:
-                continue
-            f = [x.strip() for x in ln.split(',')]
-            if len(f) < 9:
-                continue
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+        elif self.proc is not None:
+            self.proc.terminate()
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower().startswith('active'):
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        else:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['clock sampling unavailable'],
+                    'samples': 0}
+        lo, hi = self.window
+        sel = [x for x in self.samples if lo <= x[0] <= hi]
+        reasons = set()
+        for _, _, _, bits in sel:
+            for b, n in self.REASONS.items():
+                if bits & b:
                     reasons.add(n)
-        return {'sm_mhz': statistics.median(sm) if sm else None,
-                'sm_max_mhz': max(smax) if smax else None,
-                'reasons': sorted(reasons), 'samples': len(sm)}
+        return {'sm_mhz': statistics.median(x[1] for x in sel) if sel else None,
+                'sm_max_mhz': max(x[2] for x in sel) if sel else None,
+                'reasons': sorted(reasons), 'samples': len(sel), 'source': self.source,
+                'period_ms': self.period * 1e3 if self.source == 'nvml' else 100.0}
 
 
 def measured_peak():
@@ -167,24 +249,76 @@ def committed_traffic(workload: str, kernel: str):
         return None
 
 
-def cpu_baseline(ls, n_frames: int, repeats: int = 3):
-    """The oracle (reference CPU algorithm, C port) on the first frames, all threads."""
+def cpu_model() -> str:
+    """the host CPU's model name (lscpu, else /proc/cpuinfo, else platform)"""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith('Model name:'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open('/proc/cpuinfo') as fh:
+            for line in fh:
+                if line.lower().startswith('model name'):
+                    return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def time_oracle(ls, n_frames: int, threads: int, repeats: int):
+    """best-of-`repeats` seconds of the oracle (the reference CPU algorithm, C port) on
+    the first `n_frames` frames with `threads` threads; `out` is allocated and touched
+    before the clock starts, so first-touch page faults stay outside the timed region"""
     import oracle
     from cbclib_v2_gb300 import workloads
     n_frames = ls.shape[0] if n_frames <= 0 else min(n_frames, ls.shape[0])
     sub = workloads.frames_subset(ls, list(range(n_frames)))
     lines = sub.lines.astype(np.float32)
-    threads = len(os.sched_getaffinity(0))
     best = float('inf')
     for _ in range(repeats):
         out = np.zeros(sub.shape, np.float32)
+        out.fill(0.0)
         t0 = time.perf_counter()
         oracle.draw_lines(out, lines, sub.idxs, sub.max_val, sub.kernel, sub.overlap, threads)
         best = min(best, time.perf_counter() - t0)
-    return {'value': sub.n_lines / best / 1e6, 'unit': 'Mlines/s', 'cores': threads,
-            'kind': 'port', 'seconds': best, 'lines': sub.n_lines,
-            'sample': f'{sub.shape[0]} of {ls.shape[0]} frames ({sub.n_lines} lines), '
-                      f'best of {repeats}'}
+    return {'seconds': best, 'lines': sub.n_lines, 'frames': n_frames}
+
+
+def cpu_child(args):
+    """--cpu-child: time_oracle in this fresh process, one JSON line on stdout"""
+    from cbclib_v2_gb300 import workloads
+    ls = workloads.detector_stack(seed=args.seed, F=args.frames)
+    print(json.dumps(time_oracle(ls, args.cpu_frames, args.cpu_threads, args.repeats)),
+          flush=True)
+
+
+def cpu_baseline(args, rank: int):
+    """The oracle on the host cores, each measurement in a fresh interpreter (started
+    with subprocess, no CUDA context, no torch thread pools): all threads on the whole
+    stack (best of 3) and one thread on the first 8 frames"""
+    threads = len(os.sched_getaffinity(0))
+
+    def child(frames, thr, repeats):
+        cmd = [sys.executable, os.path.abspath(__file__), '--cpu-child',
+               '--frames', str(args.frames), '--seed', str(1000 + rank),
+               '--cpu-frames', str(frames), '--cpu-threads', str(thr), '--repeats', str(repeats)]
+        out = subprocess.run(cmd, capture_output=True, text=True, timeout=900, check=True)
+        return json.loads(out.stdout.strip().splitlines()[-1])
+
+    allc = child(args.cpu_frames, threads, 3)
+    one = child(8, 1, 1)
+    return {'value': allc['lines'] / allc['seconds'] / 1e6, 'unit': 'Mlines/s',
+            'cores': threads, 'kind': 'port',
+            'sample': f"{allc['frames']} of {args.frames} frames ({allc['lines']} lines), best "
+                      "of 3, out zeroed and touched before the clock, fresh process",
+            'cpu_model': cpu_model(),
+            'one_thread': {'value': one['lines'] / one['seconds'] / 1e6, 'unit': 'Mlines/s',
+                           'cores': 1,
+                           'sample': f"{one['frames']} frames ({one['lines']} lines), one run"}}
 
 
 def run_reference(args, ls, world, rank):
@@ -192,24 +326,22 @@ def run_reference(args, ls, world, rank):
         return
     import oracle  # noqa: F401  (builds the C port on first use)
     cfg = workload_config(ls)
+    threads = len(os.sched_getaffinity(0))
     frames = args.cpu_frames
     for _ in range(max(args.warmup, 1)):
-        probe = cpu_baseline(ls, 2, repeats=1)
+        probe = time_oracle(ls, 2, threads, 1)
     if frames <= 0:
         # about 60 s of CPU work over all timed steps, at least one frame per step
         per_frame = probe['seconds'] / 2
         frames = int(min(ls.shape[0], max(1, round(60.0 / max(args.steps, 1) / per_frame))))
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(ls, frames, repeats=1))
+    vals = [time_oracle(ls, frames, threads, 1) for _ in range(args.steps)]
     secs = sum(v['seconds'] for v in vals)
     lines = sum(v['lines'] for v in vals)
     value = lines / secs / 1e6
-    cb = dict(vals[0])
-    cb['value'] = value
-    cb['sample'] = f'the first {frames} of {ls.shape[0]} frames per step'
-    cb.pop('seconds', None)
-    cb.pop('lines', None)
+    cb = {'value': value, 'unit': 'Mlines/s', 'cores': threads, 'kind': 'port',
+          'sample': f'the first {frames} of {ls.shape[0]} frames per step, out zeroed and '
+                    'touched before the clock',
+          'cpu_model': cpu_model()}
     print(json.dumps({
         'impl': 'reference', 'metric': 'draw_lines throughput', 'value': value,
         'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
@@ -228,12 +360,14 @@ def workload_config(ls):
             'l2': 'output frames (%.2f GB) exceed L2; no flush' % (F * H * W * 4 / 1e9)}
 
 
-def run_fit(args, world, rank, local):
-    """forward + loss + adjoint iterations/s on the 8 x 1024^2 workload, next to the
-    cost of a finite-difference gradient from the plain forward (2 forwards per
-    parameter, 5 parameters per line)"""
+def measure_fit(steps: int, warmup: int, rank: int, local: int, fd_params: int = 32):
+    """forward + loss + adjoint iterations on the 8 x 1024^2 workload, next to a
+    finite-difference gradient from the plain forward: 2 forwards and a loss per
+    parameter, 5 parameters per line.  The finite differences of `fd_params`
+    parameters are run and timed (the whole stack per forward, and the parameter's own
+    frame only), the full gradient's cost is that time scaled to 5 N parameters."""
     import torch
-    from cbclib_v2_gb300 import _native, autograd, draw_lines, fit, workloads
+    from cbclib_v2_gb300 import autograd, draw_lines, fit, workloads
     torch.cuda.set_device(local)
     ls = workloads.fit_stack(seed=2000 + rank)
     truth = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
@@ -262,56 +396,122 @@ def run_fit(args, world, rank, local):
     stream = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def timed(fn):
-        for _ in range(args.warmup):
+    def timed(fn, k):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         a.record(stream)
-        for _ in range(args.steps):
+        for _ in range(k):
             r = fn()
         b.record(stream)
         torch.cuda.synchronize()
-        return a.elapsed_time(b) / args.steps, r
+        return a.elapsed_time(b) / k, r
 
-    ms_iter, _ = timed(fused_step)                 # forward + fused loss adjoint
-    ms_autograd, loss = timed(step)                # torch autograd and a torch loss
-    # one plain forward, the unit of a finite-difference gradient
+    ms_iter, _ = timed(fused_step, steps)           # forward + fused loss adjoint
+    ms_autograd, loss = timed(step, max(steps // 4, 3))   # torch autograd, torch loss
     out = torch.zeros(ls.shape, device='cuda')
-    for _ in range(3):
+
+    def forward():
         out.zero_()
         draw_lines(out, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
-    torch.cuda.synchronize()
-    a.record(stream)
-    for _ in range(args.steps):
+
+    ms_fwd, _ = timed(forward, steps)
+    # finite differences, really run: parameter j of line i moved by +-1e-3 px
+    h = 1e-3
+    rng = np.random.default_rng(11)
+    sel = rng.choice(ls.n_lines * 5, size=fd_params, replace=False)
+    p = truth.clone()
+    fd = torch.empty(fd_params, dtype=torch.float64, device='cuda')
+    offs = ls.frame_offsets()
+
+    def loss_of(q):
         out.zero_()
-        draw_lines(out, truth, idxs, ls.max_val, ls.kernel, ls.overlap)
-    b.record(stream)
+        draw_lines(out, q, idxs, ls.max_val, ls.kernel, ls.overlap)
+        return ((out - target) ** 2).sum(dtype=torch.float64)
+
+    def fd_whole():
+        for k, j in enumerate(sel):
+            i, c = divmod(int(j), 5)
+            p[i, c] += h
+            lp = loss_of(p)
+            p[i, c] -= 2 * h
+            lm = loss_of(p)
+            p[i, c] += h
+            fd[k] = (lp - lm) / (2 * h)
+
+    frame_out = torch.zeros(ls.shape[1:], device='cuda')
+
+    def fd_frame():
+        for k, j in enumerate(sel):
+            i, c = divmod(int(j), 5)
+            f = int(ls.idxs[i])
+            q = p[offs[f]:offs[f + 1]]
+            t = target[f]
+            vals = []
+            for sgn in (1, -1):
+                p[i, c] += sgn * h
+                frame_out.zero_()
+                draw_lines(frame_out, q, None, ls.max_val, ls.kernel, ls.overlap)
+                vals.append(((frame_out - t) ** 2).sum(dtype=torch.float64))
+                p[i, c] -= sgn * h
+            fd[k] = (vals[0] - vals[1]) / (2 * h)
+
+    fd_whole()
     torch.cuda.synchronize()
-    ms_fwd = a.elapsed_time(b) / args.steps
-    fd_ms = 2 * 5 * ls.n_lines * ms_fwd
+    t0 = time.perf_counter()
+    fd_whole()
+    torch.cuda.synchronize()
+    ms_fd_whole = (time.perf_counter() - t0) * 1e3 / fd_params
+    fd_frame()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fd_frame()
+    torch.cuda.synchronize()
+    ms_fd_frame = (time.perf_counter() - t0) * 1e3 / fd_params
+    n_params = 5 * ls.n_lines
+    return {
+        'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+        'kernel': ls.kernel, 'overlap': ls.overlap,
+        'loss': 'sum((I - target)^2), target = Poisson(render(perturbed lines))',
+        'metric': 'forward+adjoint iterations/s', 'value': 1e3 / ms_iter, 'unit': 'iter/s',
+        'ms_per_iter': ms_iter, 'steps': steps,
+        'path': 'fused: draw_lines + squared-loss adjoint (2 (I - T) per drawn pixel)',
+        'autograd_ms_per_iter': ms_autograd, 'forward_ms': ms_fwd,
+        'finite_difference': {
+            'step_px': h, 'params_run': fd_params, 'params_total': n_params,
+            'ms_per_param_whole_stack': ms_fd_whole,
+            'ms_per_param_own_frame': ms_fd_frame,
+            'gradient_ms_whole_stack': ms_fd_whole * n_params,
+            'gradient_ms_own_frame': ms_fd_frame * n_params,
+            'how': 'measured on the parameters run (2 forwards + a float64 loss each, '
+                   'wall clock with the GPU synchronised), scaled to 5 N parameters'},
+        'speedup_vs_finite_difference': ms_fd_whole * n_params / ms_iter,
+        'speedup_vs_finite_difference_own_frame': ms_fd_frame * n_params / ms_iter,
+        'loss_value': float(loss.item())}
+
+
+def run_fit(args, world, rank, local):
+    r = measure_fit(args.steps, args.warmup, rank, local)
     if rank == 0:
         print(json.dumps({
-            'metric': 'forward+adjoint iterations/s', 'value': 1e3 / ms_iter * world,
+            'metric': 'forward+adjoint iterations/s', 'value': r['value'] * world,
             'unit': 'iter/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': ms_iter, 'higher_is_better': True, 'scaling': 'weak',
+            'ms_per_step': r['ms_per_iter'], 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
-                       'kernel': ls.kernel, 'overlap': ls.overlap,
-                       'loss': 'sum((I - target)^2), target = Poisson(render(perturbed))'},
-            'path': 'fused: draw_lines + squared-loss adjoint (2 (I - T) per drawn pixel)',
-            'autograd_ms_per_iter': ms_autograd,
-            'forward_ms': ms_fwd,
-            'finite_difference_gradient_ms': fd_ms,
-            'speedup_vs_finite_difference': fd_ms / ms_iter,
-            'loss': float(loss.item())}), flush=True)
+            'config': {k: r[k] for k in ('workload', 'frames', 'lines', 'kernel', 'overlap',
+                                         'loss')},
+            **{k: r[k] for k in ('path', 'autograd_ms_per_iter', 'forward_ms',
+                                 'finite_difference', 'speedup_vs_finite_difference',
+                                 'speedup_vs_finite_difference_own_frame')}}), flush=True)
 
 
-def run_ragged(args, world, rank, local):
+def measure_ragged(steps: int, warmup: int, rank: int, local: int):
     """256 frames of 1024^2, lognormal(median 1,500, sigma 1) segments per frame clipped
     to [100, 20,000], triangular, sum: one graph replay of the autotuned CSR draw per
-    step, against one public draw_lines call per frame"""
+    step, against one eager draw_lines_csr call of the same stack and one public
+    draw_lines call per frame"""
     import torch
-    from cbclib_v2_gb300 import batch, workloads
+    from cbclib_v2_gb300 import batch, ndimage, workloads
     torch.cuda.set_device(local)
     ls = workloads.ragged_stack(seed=3000 + rank)
     offs = ls.frame_offsets()
@@ -320,42 +520,55 @@ def run_ragged(args, world, rank, local):
                              overlap=ls.overlap)
     r(lines)
     r.check()
-    for _ in range(args.warmup):
-        r.replay()
-    torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(args.steps):
-        r.replay()
-    b.record(stream)
-    torch.cuda.synchronize()
-    ms_graph = a.elapsed_time(b) / args.steps
+
+    def timed(fn, k):
+        for _ in range(max(warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(k):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    ms_graph = timed(r.replay, steps)
     r.check()
     out = torch.zeros(ls.shape, device='cuda')
-    batch.render_per_frame(out, lines, offs, ls.max_val, ls.kernel, ls.overlap)
-    torch.cuda.synchronize()
-    k = max(2, args.steps // 5)
-    a.record(stream)
-    for _ in range(k):
-        batch.render_per_frame(out, lines, offs, ls.max_val, ls.kernel, ls.overlap)
-    b.record(stream)
-    torch.cuda.synchronize()
-    ms_frames = a.elapsed_time(b) / k
+    d_offs = torch.from_numpy(offs).cuda()
+    ms_eager = timed(lambda: ndimage.draw_lines_csr(out, lines, d_offs, ls.max_val, ls.kernel,
+                                                    ls.overlap, tuning=r.tuning), steps)
+    ms_frames = timed(lambda: batch.render_per_frame(out, lines, offs, ls.max_val, ls.kernel,
+                                                     ls.overlap), max(2, steps // 10))
     t = r.tuning
+    return {
+        'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+        'lines_per_frame_min_max': [int(np.diff(offs).min()), int(np.diff(offs).max())],
+        'kernel': ls.kernel, 'overlap': ls.overlap,
+        'metric': 'ragged draw_lines throughput', 'value': ls.n_lines / ms_graph / 1e3,
+        'unit': 'Mlines/s', 'ms_graph_replay': ms_graph, 'steps': steps,
+        'autotuned': {f: getattr(t, f) for f, _ in type(t)._fields_} if t is not None else None,
+        'autotune_ms': r.timings,
+        'ms_eager_csr_call': ms_eager, 'ms_per_frame_launches': ms_frames,
+        'graph_speedup_vs_eager_csr_call': ms_eager / ms_graph,
+        'graph_speedup_vs_per_frame': ms_frames / ms_graph}
+
+
+def run_ragged(args, world, rank, local):
+    r = measure_ragged(args.steps, args.warmup, rank, local)
     if rank == 0:
         print(json.dumps({
-            'metric': 'ragged draw_lines throughput', 'value': world * ls.n_lines / ms_graph / 1e3,
-            'unit': 'Mlines/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': ms_graph, 'higher_is_better': True, 'scaling': 'weak',
+            'metric': r['metric'], 'value': world * r['value'], 'unit': 'Mlines/s',
+            'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': r['ms_graph_replay'], 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
-                       'lines_per_frame_min_max': [int(np.diff(offs).min()), int(np.diff(offs).max())],
-                       'kernel': ls.kernel, 'overlap': ls.overlap},
-            'autotuned': {f: getattr(t, f) for f, _ in type(t)._fields_} if t is not None else None,
-            'autotune_ms': r.timings,
-            'per_frame_launches_ms': ms_frames,
-            'graph_speedup_vs_per_frame': ms_frames / ms_graph}), flush=True)
+            'config': {k: r[k] for k in ('workload', 'frames', 'lines',
+                                         'lines_per_frame_min_max', 'kernel', 'overlap')},
+            **{k: r[k] for k in ('autotuned', 'autotune_ms', 'ms_eager_csr_call',
+                                 'ms_per_frame_launches', 'graph_speedup_vs_eager_csr_call',
+                                 'graph_speedup_vs_per_frame')}}), flush=True)
 
 
 def _device_steps(fn, args, local):
@@ -484,18 +697,22 @@ def run_f64(args, world, rank, local):
             'clocks': clocks, 'gpu_launches': prof.launches, 'cpu_baseline': cb}), flush=True)
 
 
-def run_fit_loop(args, world, rank, local):
+def measure_fit_loop(steps: int, warmup: int, rank: int, local: int, frames: int = 32,
+                     split=None):
     """the streak-fit loop: 32 frames of 2167x2070, 5,000 biweight lines per frame,
     max overlap; the target is Poisson noise on the render of the true lines (peak 100
-    counts), the start is the truth
-    perturbed by N(0, 1 px) on the endpoints and N(0, 0.3 px) on the widths; 100 Adam
-    steps of lr 0.05 (--steps overrides the count); reports steps/s and the parameter
-    RMS against the truth before and after"""
+    counts), the start is the truth perturbed by N(0, 1 px) on the endpoints and
+    N(0, 0.3 px) on the widths; `steps` Adam steps of lr 0.05; steps/s and the
+    parameter RMS against the truth before and after.  `split` = (rank, world)
+    fits only this rank's share of the frames (shard.partition_frames)."""
     import torch
     from cbclib_v2_gb300 import draw_lines, fit, workloads
     torch.cuda.set_device(local)
-    frames = args.frames if args.frames_given else 32
-    ls = workloads.fit_loop_stack(seed=4000 + rank, F=frames)
+    ls = workloads.fit_loop_stack(seed=4000 + (0 if split else rank), F=frames)
+    if split is not None:
+        from cbclib_v2_gb300 import shard
+        sh = shard.shard_of(ls.frame_offsets(), *split)
+        ls = workloads.frames_subset(ls, list(range(sh.f0, sh.f1)))
     dev = torch.device('cuda', local)
     truth = torch.from_numpy(ls.lines.astype(np.float32)).to(dev)
     idxs = torch.from_numpy(ls.idxs.astype(np.int32)).to(dev)
@@ -505,9 +722,8 @@ def run_fit_loop(args, world, rank, local):
     target = torch.poisson(target, generator=gen)          # counts, peak 100 per line
     start = torch.from_numpy(workloads.perturbed(ls.lines, 4100 + rank, 1.0, 0.3)
                              .astype(np.float32)).to(dev)
-    steps = args.steps if args.steps_given else 100
     fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel,
-                  overlap=ls.overlap, steps=max(args.warmup, 1), lr=0.05)      # warm-up
+                  overlap=ls.overlap, steps=max(warmup, 1), lr=0.05)      # warm-up
     res = fit.fit_lines(target, start, idxs, max_val=ls.max_val, kernel=ls.kernel,
                         overlap=ls.overlap, steps=steps, lr=0.05)
 
@@ -516,23 +732,47 @@ def run_fit_loop(args, world, rank, local):
         return {'endpoints_px': float(d[:, :4].pow(2).mean().sqrt()),
                 'width_px': float(d[:, 4].pow(2).mean().sqrt())}
 
+    return {
+        'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
+        'kernel': ls.kernel, 'overlap': ls.overlap, 'lr': 0.05,
+        'loss': 'sum((I - T)^2), T = Poisson(render of the true lines), peak 100 counts',
+        'start': 'truth + N(0, 1 px) endpoints, N(0, 0.3 px) widths',
+        'metric': 'streak-fit Adam steps/s', 'value': 1e3 / res.ms_per_step,
+        'unit': 'steps/s', 'ms_per_step': res.ms_per_step, 'steps': steps,
+        'rms_start': rms(start), 'rms_final': rms(res.lines),
+        'loss_start': res.losses[0], 'loss_final': res.losses[-1]}
+
+
+def run_fit_loop(args, world, rank, local):
+    frames = args.frames if args.frames_given else 32
+    steps = args.steps if args.steps_given else 100
+    split = (rank, world) if (args.shard and world > 1) else None
+    r = measure_fit_loop(steps, args.warmup, rank, local, frames, split)
     if rank == 0:
         print(json.dumps({
-            'metric': 'streak-fit Adam steps/s', 'value': world * 1e3 / res.ms_per_step,
+            'metric': r['metric'], 'value': (world if split is None else 1) * r['value'],
             'unit': 'steps/s', 'n_gpus': world, 'steps': steps, 'warmup': args.warmup,
-            'ms_per_step': res.ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
-            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': ls.name, 'frames': ls.shape[0], 'lines': ls.n_lines,
-                       'kernel': ls.kernel, 'overlap': ls.overlap, 'lr': 0.05,
-                       'loss': 'sum((I - T)^2), T = Poisson(render of the true lines), '
-                               'peak 100 counts',
-                       'start': 'truth + N(0, 1 px) endpoints, N(0, 0.3 px) widths'},
-            'rms_start': rms(start), 'rms_final': rms(res.lines),
-            'loss_start': res.losses[0], 'loss_final': res.losses[-1]}), flush=True)
+            'ms_per_step': r['ms_per_step'], 'higher_is_better': True,
+            'scaling': 'strong' if split else 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic',
+            'config': {k: r[k] for k in ('workload', 'frames', 'lines', 'kernel', 'overlap',
+                                         'lr', 'loss', 'start')},
+            **{k: r[k] for k in ('rms_start', 'rms_final', 'loss_start', 'loss_final')}}),
+            flush=True)
+
+
+def e2e_step_bytes(n_lines: int, drawn: int):
+    """bytes across the link per step: lines (5 float32) and int32 indices up, the
+    drawn pixels read and written in place in the host frames"""
+    return {'h2d_bytes_per_step': int(n_lines * 20 + n_lines * 4 + drawn * 4),
+            'd2h_bytes_per_step': int(drawn * 4)}
 
 
 def main():
     args = parse()
+    if args.cpu_child:
+        cpu_child(args)
+        return
     world, rank, local = dist_env()
     if args.workload == 'fit_loop' and args.impl == 'gb300':
         run_fit_loop(args, world, rank, local)
@@ -549,13 +789,15 @@ def main():
     if args.workload == 'ragged' and args.impl == 'gb300':
         run_ragged(args, world, rank, local)
         return
-    import torch
-    from cbclib_v2_gb300 import _native, draw_lines, ndimage, workloads
+    from cbclib_v2_gb300 import workloads
 
-    ls = workloads.detector_stack(seed=1000 + rank, F=args.frames)
+    split = args.shard and world > 1
+    ls = workloads.detector_stack(seed=1000 + (0 if split else rank), F=args.frames)
     if args.impl == 'reference':
         run_reference(args, ls, world, rank)
         return
+    import torch
+    from cbclib_v2_gb300 import _native, draw_lines, ndimage, shard
 
     dist = None
     if world > 1:
@@ -563,6 +805,11 @@ def main():
         dist.init_process_group('nccl', init_method='env://')
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
+    full_lines = ls.n_lines
+    if split:
+        # this rank's contiguous frame range of the one stack, balanced by line counts
+        sh = shard.shard_of(ls.frame_offsets(), rank, world)
+        ls = workloads.frames_subset(ls, list(range(sh.f0, sh.f1)))
     F, H, W = ls.shape
     N = ls.n_lines
     lines = torch.from_numpy(ls.lines.astype(np.float32)).to(dev)
@@ -573,12 +820,18 @@ def main():
         if dist is not None:
             dist.barrier(device_ids=[local])
 
-    for _ in range(args.warmup):
-        draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
-    torch.cuda.synchronize()
+    def max_over_ranks(ms):
+        if dist is None:
+            return ms
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
 
     clocks = ClockSampler(local)
     clocks.start()
+    for _ in range(args.warmup):
+        draw_lines(out, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
+    torch.cuda.synchronize()
     _native.profile_enable(True)
     _native.profile_read(reset=True)
     barrier()
@@ -597,51 +850,67 @@ def main():
     strategy = ndimage.last_status(dev).strategy
     _native.profile_enable(False)
     clk = clocks.stop()
-    ms = t0.elapsed_time(t1)
-    if dist is not None:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    ms_step = ms / args.steps
-    value = world * N / (ms_step * 1e-3) / 1e6
+    ms_step = max_over_ranks(t0.elapsed_time(t1)) / args.steps
+    total_lines = full_lines if split else world * N
+    value = total_lines / (ms_step * 1e-3) / 1e6
 
-    # end to end through the public API with pinned host buffers
-    e2e = None
-    if not args.no_e2e:
-        h_out = torch.zeros(ls.shape, dtype=torch.float32).pin_memory()
-        h_lines = torch.from_numpy(ls.lines.astype(np.float32)).pin_memory()
-        h_idxs = torch.from_numpy(ls.idxs.astype(np.int32)).pin_memory()
+    # the drawn pixels (the bytes that cross the link in place, and the sparse model)
+    ref = torch.zeros(ls.shape, dtype=torch.float32, device=dev)
+    draw_lines(ref, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
+    drawn = int((ref != 0).sum())
+    drawn_sectors = int(ref.reshape(-1, 8).ne(0).any(dim=1).sum().item())
+    del ref
+
+    def e2e_run(h_out, h_lines, h_idxs, what):
         for _ in range(max(1, args.warmup)):
             draw_lines(h_out, h_lines, h_idxs, ls.max_val, ls.kernel, ls.overlap)
         e_steps = max(3, min(args.steps // 4, 50))
         barrier()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
         a.record(stream)
         for _ in range(e_steps):
             draw_lines(h_out, h_lines, h_idxs, ls.max_val, ls.kernel, ls.overlap)
         b.record(stream)
         torch.cuda.synchronize()
+        wall = (time.perf_counter() - w0) * 1e3 / e_steps
         barrier()
-        e_ms = a.elapsed_time(b) / e_steps
-        if dist is not None:
-            tt = torch.tensor([e_ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e_ms = float(tt.item())
-        # the frames stay in page-locked host memory: the library's kernels read and
-        # write the drawn pixels there through their device mapping (NVLink-C2C), so
-        # the bytes across the link per step are the lines and indices up, and the
-        # drawn pixels read and written in place (counted from a draw into zeros)
-        ref = torch.zeros(ls.shape, dtype=torch.float32, device=dev)
-        draw_lines(ref, lines, idxs, ls.max_val, ls.kernel, ls.overlap)
-        drawn = int((ref != 0).sum())
-        del ref
-        e2e = {'value': world * N / (e_ms * 1e-3) / 1e6, 'unit': 'Mlines/s',
-               'ms_per_step': e_ms,
-               'h2d_bytes_per_step': int(h_lines.numel() * 4 + h_idxs.numel() * 4 + drawn * 4),
-               'd2h_bytes_per_step': int(drawn * 4),
-               'frames': 'page-locked host memory, drawn pixels combined in place by the '
-                         'kernels (zero-copy); %d of %d pixels drawn' % (drawn, h_out.numel())}
+        e_ms = max_over_ranks(a.elapsed_time(b) / e_steps)
+        return {'value': total_lines / (e_ms * 1e-3) / 1e6, 'unit': 'Mlines/s',
+                'ms_per_step': e_ms, 'wall_ms_per_step': wall, 'steps': e_steps,
+                **e2e_step_bytes(N, drawn),
+                'frames': what + '; %d of %d pixels drawn' % (drawn, F * H * W)}
+
+    # end to end through the public API with host buffers: NumPy arrays (what the
+    # reference's callers pass), then page-locked torch tensors
+    e2e = e2e_pinned = None
+    if not args.no_e2e:
+        n_out = np.zeros(ls.shape, np.float32)
+        n_out.fill(0.0)
+        n_lines = np.ascontiguousarray(ls.lines.astype(np.float32))
+        n_idxs = np.ascontiguousarray(ls.idxs.astype(np.int32))
+        mode = _native.host_access(n_out.ctypes.data)
+        e2e = e2e_run(n_out, n_lines, n_idxs,
+                      'NumPy arrays in pageable host memory, drawn pixels combined in place '
+                      'by the kernels (zero-copy over NVLink-C2C)' if mode == _native.HOST_PAGEABLE
+                      else 'NumPy arrays, copied to the device and back')
+        del n_out
+        h_out = torch.zeros(ls.shape, dtype=torch.float32).pin_memory()
+        h_lines = torch.from_numpy(ls.lines.astype(np.float32)).pin_memory()
+        h_idxs = torch.from_numpy(ls.idxs.astype(np.int32)).pin_memory()
+        e2e_pinned = e2e_run(h_out, h_lines, h_idxs,
+                             'page-locked torch tensors, drawn pixels combined in place by '
+                             'the kernels (zero-copy)')
+        del h_out
+
+    extra = {}
+    if not args.headline_only:
+        steps_x = max(args.steps, 20)
+        extra['forward_adjoint'] = measure_fit(min(steps_x, 200), max(args.warmup, 3), rank, local)
+        extra['ragged_graph'] = measure_ragged(min(steps_x, 100), max(args.warmup, 3), rank,
+                                               local)
+        extra['fit_loop'] = measure_fit_loop(100, max(args.warmup, 3), rank, local)
 
     if rank != 0:
         if dist is not None:
@@ -651,17 +920,18 @@ def main():
     peak, peak_src = measured_peak()
     render_ms = prof.ms_render / max(prof.calls, 1)
     kname = 'segments_kernel' if strategy == _native.STRATEGY_LINES else 'render_kernel'
-    # bytes the op must move: every 32-byte sector of `out` holding a drawn pixel is
-    # read and written once (all other sectors are untouched), plus each line's
-    # 5 coordinates and frame index
-    drawn_sectors = int(out.reshape(-1, 8).ne(0).any(dim=1).sum().item())
+    # bytes the op must move: the in-place contract reads and writes every output pixel
+    # once, plus each line's 5 coordinates and frame index; the sparse model counts the
+    # 32-byte sectors holding a drawn pixel (all other sectors are untouched)
     algo_bytes = 64 * drawn_sectors + N * 24
     full_bytes = 2 * F * H * W * 4 + N * 24
     achieved = full_bytes / (render_ms * 1e-3) / 1e9
     sparse = algo_bytes / (render_ms * 1e-3) / 1e9
+    traffic = committed_traffic(ls.name, kname) if not split else None
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_src,
-                'traffic': committed_traffic(ls.name, kname), 'kernel': kname,
+                'traffic': traffic, 'kernel': kname,
+                'traffic_frac': (traffic / (render_ms * 1e-3) / 1e9 / peak) if traffic else None,
                 'algorithmic_bytes': full_bytes,
                 'bytes_model': 'read + write of every output pixel (the call updates out '
                                'in place) + 24 B per line: 2*F*H*W*4 + 24*N',
@@ -677,19 +947,21 @@ def main():
                     'offsets': prof.ms_offsets / max(prof.calls, 1),
                     'fill': prof.ms_fill / max(prof.calls, 1),
                     'render': render_ms}}
+    cfg = workload_config(ls)
+    if split:
+        cfg['sharding'] = f'one {args.frames}-frame stack split by frames across {world} ranks'
     res = {
         'metric': 'draw_lines throughput', 'value': value, 'unit': 'Mlines/s', 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-        'data': 'synthetic', 'config': workload_config(ls), 'roofline': roofline,
+        'higher_is_better': True, 'scaling': 'strong' if split else 'weak', 'vs_baseline': None,
+        'dtype': 'f32', 'data': 'synthetic', 'config': cfg, 'roofline': roofline,
         'output_gbs': F * H * W * 4 / (ms_step * 1e-3) / 1e9, 'clocks': clk,
-        'gpu_launches': prof.launches, 'e2e': e2e,
+        'gpu_launches': prof.launches, 'e2e': e2e, 'e2e_pinned': e2e_pinned,
     }
+    if extra:
+        res['workloads'] = extra
     if not args.no_cpu_baseline and world == 1:
-        cb = cpu_baseline(ls, args.cpu_frames, repeats=2)
-        cb.pop('seconds', None)
-        cb.pop('lines', None)
-        res['cpu_baseline'] = cb
+        res['cpu_baseline'] = cpu_baseline(args, rank)
     print(json.dumps(res), flush=True)
     if dist is not None:
         dist.destroy_process_group()

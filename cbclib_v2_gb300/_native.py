@@ -63,7 +63,10 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_squared_loss_step_workspace_size', 'cbc_squared_loss_step_f32',
            'cbc_squared_loss_step_sum_f32',
            'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status',
-           'cbc_adam_step_f32', 'cbc_draw_lines_host_f32', 'cbc_draw_lines_host_f64')
+           'cbc_adam_step_f32', 'cbc_draw_lines_host_f32', 'cbc_draw_lines_host_f64',
+           'cbc_host_access')
+
+HOST_NONE, HOST_MAPPED, HOST_PAGEABLE = 0, 1, 2
 
 NO_WINNER = 0x7f7f7f7f
 
@@ -163,6 +166,8 @@ def _declare(lib):
     lib.cbc_last_error.restype = ctypes.c_char_p
     lib.cbc_version.argtypes = []
     lib.cbc_version.restype = ctypes.c_char_p
+    lib.cbc_host_access.argtypes = [p, ctypes.POINTER(i32)]
+    lib.cbc_host_access.restype = ctypes.c_int
 
 
 def library_path() -> str:
@@ -187,6 +192,16 @@ def lib():
 def last_error() -> str:
     msg = lib().cbc_last_error()
     return msg.decode() if msg else ''
+
+
+def host_access(ptr: int) -> int:
+    """HOST_MAPPED, HOST_PAGEABLE or HOST_NONE: how the current device reaches the host
+    memory at ``ptr`` (cbc_host_access)"""
+    mode = ctypes.c_int32(HOST_NONE)
+    rc = lib().cbc_host_access(ctypes.c_void_p(ptr), ctypes.byref(mode))
+    if rc:
+        raise RuntimeError(f"cbc_host_access failed: {last_error()}")
+    return int(mode.value)
 
 
 def profile_enable(on: bool) -> bool:

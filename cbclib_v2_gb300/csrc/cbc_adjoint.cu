@@ -65,25 +65,25 @@ struct WinnerAct {
     }
 };
 
-/* per-line constants of the pixel terms.  With c = (cx, cy) the segment centre,
- * tau = (t0, t1) = p1 - p0 and rmag = 1 / |tau|^2, the nearest point of the segment
- * to pixel P is c + t tau, t = (P - c) . tau rmag clamped to [-1/2, 1/2]; with d the
- * distance to it, kappa(d^2) is k0 + k1 d^2 (biweight, parabolic), k0 exp(k1 d^2)
- * (gaussian), k0 / d (triangular, 0 at d = 0) or 0 (rectangular); rw = 1 / w. */
+/* per-line constants of the pixel terms: the segment's end points p0 = (x0, y0) and
+ * p1 = (x1, y1) as given, rmag = 1 / |p1 - p0|^2, and kappa(d^2) = k0 + k1 d^2
+ * (biweight, parabolic), k0 exp(k1 d^2) (gaussian), k0 / d (triangular, 0 at d = 0)
+ * or 0 (rectangular); rw = 1 / w. */
 template <typename T>
 struct alignas(8 * sizeof(T)) GradCoef {
-    T cx, cy, t0, t1, rmag, k0, k1, rw;
+    T x0, y0, x1, y1, rmag, k0, k1, rw;
 };
 
-/* the constants of a line from its start point, tangent and width */
+/* the constants of a line from its end points and width */
 template <typename T, int K>
-__device__ __forceinline__ GradCoef<T> make_grad_coef(T x0, T y0, T t0, T t1, T w, T max_val)
+__device__ __forceinline__ GradCoef<T> make_grad_coef(T x0, T y0, T x1, T y1, T w, T max_val)
 {
     GradCoef<T> c;
-    c.t0 = t0;
-    c.t1 = t1;
-    c.cx = x0 + T(0.5) * t0;
-    c.cy = y0 + T(0.5) * t1;
+    c.x0 = x0;
+    c.y0 = y0;
+    c.x1 = x1;
+    c.y1 = y1;
+    const T t0 = x1 - x0, t1 = y1 - y0;
     c.rmag = T(1) / (t0 * t0 + t1 * t1);
     c.rw = T(1) / w;
     const T rww = c.rw * c.rw;
@@ -119,8 +119,7 @@ grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const T *ln = lines + i * 5;
-    const T x0 = ln[0], y0 = ln[1];
-    coef[i] = make_grad_coef<T, K>(x0, y0, ln[2] - x0, ln[3] - y0, ln[4], max_val);
+    coef[i] = make_grad_coef<T, K>(ln[0], ln[1], ln[2], ln[3], ln[4], max_val);
 }
 
 template <typename T, int K>
@@ -138,16 +137,45 @@ __device__ __forceinline__ T kappa_d2(T d2, T k0, T k1)
     }
 }
 
-/* g * dv/dtheta of one line at pixel (X, Y): v[0..4] for x0, y0, x1, y1, w */
+template <typename T> __device__ __forceinline__ T fma_rn(T a, T b, T c);
+template <> __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <> __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+/* g * dv/dtheta of one line at pixel (X, Y): v[0..4] for x0, y0, x1, y1, w.
+ * The geometry is taken relative to the pixel from the end points as given: a pixel
+ * coordinate (an integer) minus an end point is exact in T whenever the difference
+ * is below 2^p ulp(end point), so q - P has no cancellation error.  Inside the
+ * segment's extent (0 < s < 1) q - P = c (t1, -t0) rmag with c = (p0 - P) x (p1 - P),
+ * evaluated as a difference of products with an FMA error term (within 2 ulp of the
+ * exact cross product); beyond an end q is that end point.  s itself only weights the
+ * two end points, so its rounding does not cancel. */
 template <typename T, int K>
 __device__ __forceinline__ void pixel_term(const GradCoef<T> &c, T g, T X, T Y, T (&v)[5])
 {
-    T t = ((X - c.cx) * c.t0 + (Y - c.cy) * c.t1) * c.rmag;
-    t = t < T(-0.5) ? T(-0.5) : (t > T(0.5) ? T(0.5) : t);
-    const T dx = c.cx + t * c.t0 - X, dy = c.cy + t * c.t1 - Y;
-    const T d2 = dx * dx + dy * dy;
+    const T a = c.x0 - X, b = c.y0 - Y, e = c.x1 - X, f = c.y1 - Y;
+    const T t0 = e - a, t1 = f - b;
+    T s = -(a * t0 + b * t1) * c.rmag;
+    T dx, dy, d2;
+    if (s <= T(0)) {
+        s = T(0);
+        dx = a;
+        dy = b;
+        d2 = a * a + b * b;
+    } else if (s >= T(1)) {
+        s = T(1);
+        dx = e;
+        dy = f;
+        d2 = e * e + f * f;
+    } else {
+        const T be = b * e;
+        const T cr = fma_rn(a, f, -be) + fma_rn(-b, e, be);
+        const T u = cr * c.rmag;
+        dx = u * t1;
+        dy = -u * t0;
+        d2 = cr * u;
+    }
     const T G = g * kappa_d2<T, K>(d2, c.k0, c.k1);
-    const T gb = G * (t + T(0.5)), ga = G - gb;
+    const T gb = G * s, ga = G - gb;
     v[0] = ga * dx;
     v[1] = ga * dy;
     v[2] = gb * dx;
@@ -158,8 +186,9 @@ __device__ __forceinline__ void pixel_term(const GradCoef<T> &c, T g, T X, T Y, 
 /* sum overlap: every drawn pixel (error <= 1) of every line gets its term */
 template <typename T, int K>
 struct BackwardAct {
-    static constexpr bool kNeedsGeometry = true;
+    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
+    const T *lines;      /* (N, 5) parameters as given */
     const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */
     const T *image;
     const T *target;
@@ -171,9 +200,11 @@ struct BackwardAct {
     __device__ __forceinline__ void item_begin(int lane, const SlotTable<T> &S) {
         #pragma unroll
         for (int k = 0; k < 5; k++) acc[lane][k] = T(0);
-        if (S.line[lane] >= 0)
-            coef[lane] = make_grad_coef<T, K>(S.x0[lane], S.y0[lane], S.t0[lane], S.t1[lane],
-                                              S.w[lane], max_val);
+        const int line = S.line[lane];
+        if (line >= 0) {
+            const T *ln = lines + (size_t)line * 5;
+            coef[lane] = make_grad_coef<T, K>(ln[0], ln[1], ln[2], ln[3], ln[4], max_val);
+        }
     }
     __device__ __forceinline__ void item_end(int lane, const SlotTable<T> &S) {
         const int line = S.line[lane];
@@ -338,10 +369,10 @@ struct SlotPair {
         }
         mru_a = in_a;
         GradCoef<T> c;
-        c.cx = in_a ? A.c.cx : B.c.cx;
-        c.cy = in_a ? A.c.cy : B.c.cy;
-        c.t0 = in_a ? A.c.t0 : B.c.t0;
-        c.t1 = in_a ? A.c.t1 : B.c.t1;
+        c.x0 = in_a ? A.c.x0 : B.c.x0;
+        c.y0 = in_a ? A.c.y0 : B.c.y0;
+        c.x1 = in_a ? A.c.x1 : B.c.x1;
+        c.y1 = in_a ? A.c.y1 : B.c.y1;
         c.rmag = in_a ? A.c.rmag : B.c.rmag;
         c.k0 = in_a ? A.c.k0 : B.c.k0;
         c.k1 = in_a ? A.c.k1 : B.c.k1;
@@ -634,6 +665,7 @@ dense_max_kernel(DenseArgs<T> a)
 template <typename T>
 struct AdjArgs {
     DriveArgs<T> d;
+    const T *lines;
     const T *grad_out;
     const T *image;
     const T *out0;
@@ -664,6 +696,7 @@ backward_kernel(AdjArgs<T> a)
     __shared__ T acc_s[kSegWarps][32][5];
     __shared__ GradCoef<T> coef_s[kSegWarps][32];
     BackwardAct<T, K> act;
+    act.lines = a.lines;
     act.grad_out = a.grad_out;
     act.image = a.image;
     act.target = a.target;
@@ -900,6 +933,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         aa.d.W = (int)W;
         aa.d.st = st;
         aa.d.work = &st->work;
+        aa.lines = lines;
         aa.grad_out = grad_out;
         aa.image = image;
         aa.out0 = out0;
@@ -1100,6 +1134,7 @@ int sum_loss_step_impl(const float *target, float *image, long long n_frames, lo
         aa.d.W = (int)W;
         aa.d.st = st;
         aa.d.work = &st->work;
+        aa.lines = lines;
         aa.image = image;
         aa.target = target;
         aa.gacc = gacc;

@@ -633,6 +633,8 @@ int draw_lines_impl(T *out, long long n_frames, long long H, long long W, const 
         return fail(CBC_ERR_INVALID, "negative size");
     if (H > INT_MAX / 2 || W > INT_MAX / 2)
         return fail(CBC_ERR_INVALID, "frame dimensions must be below 2^30");
+    if (n_frames > INT_MAX)     /* line records hold the frame as a 32-bit index */
+        return fail(CBC_ERR_INVALID, "n_frames must not exceed 2^31 - 1");
     if (kernel < 0 || kernel > 4) return fail(CBC_ERR_INVALID, "Invalid kernel type");
     if (overlap != CBC_SUM && overlap != CBC_MAX)
         return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
@@ -881,20 +883,28 @@ int draw_lines_host_impl(T *host_out, long long n_frames, long long H, long long
     if (overlap != CBC_SUM && overlap != CBC_MAX)
         return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
     if (n > 0 && (!host_out || !scratch)) return fail(CBC_ERR_INVALID, "null pointer");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
     T *dev_host = nullptr;
     if (n > 0) {
-        /* the device address of the host frames: page-locked memory only */
+        /* the device address of the host frames: the mapping of page-locked memory, or
+         * the host address itself where the device reads and writes pageable memory
+         * coherently through the host's page tables (NVLink-C2C systems) */
         cudaError_t e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&dev_host),
                                                  host_out, 0);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return fail(CBC_ERR_INVALID, "out is not page-locked host memory the device can "
-                                         "address (" + std::string(cudaGetErrorString(e)) + ")");
+            int pageable = 0, host_tables = 0;
+            cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+            cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                   dev);
+            if (!(pageable && host_tables))
+                return fail(CBC_ERR_INVALID, "out is not host memory the device can address (" +
+                                                 std::string(cudaGetErrorString(e)) + ")");
+            dev_host = host_out;
         }
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long most = (long long)(sms > 0 ? sms : 132) * 16;
     long long blocks = (n + kThreads - 1) / kThreads;
@@ -945,6 +955,27 @@ bool draw_workspace_parts(long long n_frames, long long H, long long W, long lon
 }  // namespace cbc
 
 extern "C" {
+
+int cbc_host_access(const void *host_ptr, int32_t *mode)
+{
+    cbc::clear_error();
+    if (!mode) return cbc::fail(CBC_ERR_INVALID, "null mode pointer");
+    *mode = CBC_HOST_NONE;
+    if (!host_ptr) return CBC_OK;
+    void *mapped = nullptr;
+    if (cudaHostGetDevicePointer(&mapped, const_cast<void *>(host_ptr), 0) == cudaSuccess) {
+        *mode = CBC_HOST_MAPPED;
+        return CBC_OK;
+    }
+    cudaGetLastError();
+    int dev = 0, pageable = 0, host_tables = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    if (pageable && host_tables) *mode = CBC_HOST_PAGEABLE;
+    return CBC_OK;
+}
 
 int cbc_draw_lines_host_f32(float *host_out, int64_t n_frames, int64_t height, int64_t width,
                             const float *lines, int64_t n_lines, const void *idxs,
@@ -1177,31 +1208,19 @@ constexpr size_t kNoallocCkOffset =
     kNoallocRecOffset + (sizeof(LineRec<float>) * CBC_NOALLOC_MAX_LINES + 255) / 256 * 256;
 constexpr size_t kNoallocBytes =
     kNoallocCkOffset + sizeof(Checkpoint<float>) * CBC_NOALLOC_MAX_CHECKPOINTS;
-static_assert(sizeof(DevStatus) <= kNoallocRecOffset, "status block exceeds its slot");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[kNoallocMaxDevices] = {};
-
-/* the array's address on the current device, looked up once per device */
+/* the array's address on the current device.  Looked up on every call: the address
+ * belongs to the current context, and a context created after cudaDeviceReset may
+ * place the array elsewhere, so a cached value could go stale. */
 int noalloc_scratch(unsigned char **base)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= kNoallocMaxDevices)
-        return fail(CBC_ERR_INVALID, "device ordinal beyond the no-allocation table");
-    std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(CBC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = p;
-    }
-    *base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(CBC_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *base = static_cast<unsigned char *>(p);
     return CBC_OK;
 }
 
@@ -1214,6 +1233,8 @@ int draw_lines_noalloc(float *out, long long n_frames, long long H, long long W,
         return fail(CBC_ERR_INVALID, "negative size");
     if (H > INT_MAX / 2 || W > INT_MAX / 2)
         return fail(CBC_ERR_INVALID, "frame dimensions must be below 2^30");
+    if (n_frames > INT_MAX)     /* line records hold the frame as a 32-bit index */
+        return fail(CBC_ERR_INVALID, "n_frames must not exceed 2^31 - 1");
     if (kernel < 0 || kernel > 4) return fail(CBC_ERR_INVALID, "Invalid kernel type");
     if (overlap != CBC_SUM && overlap != CBC_MAX)
         return fail(CBC_ERR_INVALID, "Invalid overlap keyword");

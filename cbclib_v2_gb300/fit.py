@@ -17,7 +17,8 @@ import torch
 from . import _native, ndimage
 from .autograd import draw_lines_fn, squared_loss_backward
 
-__all__ = ['FitResult', 'adam_step', 'fit_lines', 'squared_loss_step']
+__all__ = ['FitResult', 'ShardedFit', 'adam_step', 'fit_lines', 'fit_lines_sharded',
+           'reduce_losses', 'shard_problem', 'squared_loss_step']
 
 
 @dataclass
@@ -286,3 +287,60 @@ def fit_lines(target: torch.Tensor, lines0: torch.Tensor, idxs: Optional[torch.T
     with torch.no_grad():
         last = float(_loss(params, idxs, target, max_val, kernel, overlap))
     return FitResult(params.detach(), steps, seconds, [first, last], history)
+
+
+@dataclass
+class ShardedFit:
+    shard: 'object'                      # shard.Shard: this rank's frames and lines
+    result: FitResult                    # this rank's fit (its lines only)
+    losses: List[float]                  # loss of the whole stack before and after
+
+
+def shard_problem(target, lines0, frame_offsets, rank: int, world: int):
+    """This rank's part of a streak fit over one stack whose lines are grouped by
+    frame (CSR ``frame_offsets``): its contiguous frame range balanced by line counts
+    (shard.shard_of), the target frames and lines of that range, and frame indices
+    rebased to its first frame.  Host logic only; returns (shard, target, lines,
+    idxs)."""
+    import numpy as np
+    from . import shard as _shard
+    offs = np.asarray(torch.as_tensor(frame_offsets).cpu(), dtype=np.int64).reshape(-1)
+    sh = _shard.shard_of(offs, rank, world)
+    local_t = target[sh.f0:sh.f1]
+    local_l = lines0[sh.l0:sh.l1]
+    counts = np.diff(sh.local_offsets(offs))
+    idxs = torch.from_numpy(np.repeat(np.arange(sh.n_frames, dtype=np.int32), counts))
+    return sh, local_t, local_l, idxs
+
+
+def reduce_losses(losses: List[float]) -> List[float]:
+    """sum of every rank's scalar losses (the only cross-rank values of a sharded fit),
+    over the default process group when one is initialised"""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return list(losses)
+    dev = (torch.device('cuda', torch.cuda.current_device())
+           if dist.get_backend() == 'nccl' else torch.device('cpu'))
+    t = torch.tensor(losses, dtype=torch.float64, device=dev)
+    dist.all_reduce(t)
+    return [float(x) for x in t.cpu()]
+
+
+def fit_lines_sharded(target, lines0, frame_offsets, rank: Optional[int] = None,
+                      world: Optional[int] = None, **kw) -> ShardedFit:
+    """fit_lines over one stack split across ranks by frames (one process per GPU):
+    each rank fits only the lines of its own frames against its own target frames, on
+    its current CUDA device; nothing is exchanged on the data path, only the two
+    scalar losses are summed.  ``rank``/``world`` default to the default process
+    group's (0 and 1 without one).  ``target`` may be a host or device tensor of the
+    whole stack; only this rank's frames are moved to the device."""
+    import torch.distributed as dist
+    if rank is None or world is None:
+        if dist.is_available() and dist.is_initialized():
+            rank, world = dist.get_rank(), dist.get_world_size()
+        else:
+            rank, world = 0, 1
+    sh, t, ln, ix = shard_problem(target, lines0, frame_offsets, rank, world)
+    dev = torch.device('cuda', torch.cuda.current_device())
+    res = fit_lines(t.to(dev), ln.to(dev), ix.to(dev), **kw)
+    return ShardedFit(sh, res, reduce_losses(res.losses))

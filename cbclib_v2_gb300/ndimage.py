@@ -17,7 +17,8 @@ import torch
 from . import _native
 from . import device as _device
 
-__all__ = ['draw_lines', 'draw_lines_csr', 'accumulate_lines', 'Workspace', 'tuning']
+__all__ = ['draw_lines', 'draw_lines_csr', 'accumulate_lines', 'Workspace', 'tuning',
+           'release_scratch']
 
 _tls = threading.local()
 
@@ -467,26 +468,57 @@ def draw_lines(out, lines, idxs=None, max_val: float = 1.0, kernel: str = 'recta
         ``out``.
     """
     k, ov = _check_names(kernel, overlap)
-    if isinstance(out, torch.Tensor) and not out.is_cuda and \
-            _draw_lines_staged(out, lines, idxs, max_val, k, ov):
+    host = _host_tensor(out)
+    if host is not None and _draw_lines_staged(host, lines, idxs, max_val, k, ov):
         return out
     return _on_device(out, 'draw_lines',
                       lambda dev_out: _draw_lines_cuda(dev_out, lines, idxs, max_val, k, ov))
 
 
+def _host_tensor(out) -> Optional[torch.Tensor]:
+    """a CPU tensor sharing the memory of a host array that the library may update in
+    place (a CPU tensor, or a writable, aligned, C-contiguous NumPy array), else None"""
+    if isinstance(out, torch.Tensor):
+        return None if out.is_cuda else out
+    if isinstance(out, np.ndarray) and out.flags.c_contiguous and out.flags.writeable and \
+            out.flags.aligned and out.dtype in (np.float32, np.float64):
+        return torch.from_numpy(out)
+    return None
+
+
+# device scratch frames of the host-frame path, per (device, stream, host thread),
+# least recently used first; at most MAX_HOST_SCRATCH are kept (release_scratch()
+# drops them all)
+MAX_HOST_SCRATCH = 4
 _host_scratch: dict = {}
+_host_scratch_lock = threading.Lock()
+
+
+def release_scratch() -> None:
+    """Drop the library's cached device buffers of this process (workspaces, the
+    host-frame scratch frames and the packed max scratch); later calls allocate them
+    again.  Waits for the current devices' work first."""
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+    with _host_scratch_lock:
+        _host_scratch.clear()
+    with _ws_lock:
+        _workspaces.clear()
+    _packed.clear()
 
 
 def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: int,
                        overlap: int) -> bool:
-    """draw_lines on page-locked host frames of 2-D lines without copying the frames:
-    the kernels draw into a device scratch holding the overlap's identity and combine
-    the drawn pixels into the host frames through their device mapping
-    (cbc_draw_lines_host_*).  The scratch (one per device, stream and host thread) is
-    left at the identity after every call; it is filled again only when the overlap,
-    the dtype or the size changes.  Returns False when the frames do not qualify
-    (pageable, non-contiguous, 3-D lines or no device)."""
-    if not (host.is_pinned() and host.is_contiguous() and host.dim() >= 2 and
+    """draw_lines on host frames of 2-D lines without copying the frames: the kernels
+    draw into a device scratch holding the overlap's identity and combine the drawn
+    pixels into the host frames in place (cbc_draw_lines_host_*), through the device
+    mapping of page-locked memory, or directly where the device reads and writes
+    pageable memory coherently (NVLink-C2C systems; NumPy arrays included).  The
+    scratch (one per device, stream and host thread) is left at the identity after
+    every call; it is filled again only when the overlap, the dtype or the size
+    changes.  Returns False when the frames do not qualify (memory the device cannot
+    address, non-contiguous, 3-D lines or no device)."""
+    if not (host.is_contiguous() and host.dim() >= 2 and host.numel() > 0 and
             host.dtype in (torch.float32, torch.float64)):
         return False
     if _device.get_device() != 'cuda':
@@ -496,6 +528,9 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
         return False
     F, H, W = _frames_of(host)
     dev = torch.device('cuda', torch.cuda.current_device())
+    with _on_current_device(dev):
+        if _native.host_access(host.data_ptr()) == _native.HOST_NONE:
+            return False
     ln = _as_device_lines(t, dev, host.dtype)
     n = ln.shape[0]
     ix = _as_device_idxs(idxs, n, dev)
@@ -508,11 +543,19 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
     with _on_current_device(dev):
         stream = _current_stream(dev)
         key = (dev.index, stream, threading.get_ident())
-        entry = _host_scratch.get(key)
         tag = (overlap, host.dtype)
-        if entry is None or entry[0].numel() < F * H * W or entry[0].dtype != host.dtype:
+        with _host_scratch_lock:
+            entry = _host_scratch.pop(key, None)
+            if entry is None or entry[0].numel() < F * H * W or entry[0].dtype != host.dtype:
+                entry = None
+                while len(_host_scratch) >= MAX_HOST_SCRATCH:
+                    _host_scratch.pop(next(iter(_host_scratch)))
+            else:
+                _host_scratch[key] = entry           # most recently used last
+        if entry is None:
             entry = [torch.empty(F * H * W, dtype=host.dtype, device=dev), None]
-            _host_scratch[key] = entry
+            with _host_scratch_lock:
+                _host_scratch[key] = entry
         scratch = entry[0]
         state = {'fill': int(entry[1] != tag)}
 

@@ -152,13 +152,15 @@ CBC_API int cbc_draw_lines_csr_f64(double *out, int64_t n_frames, int64_t height
  * limits: n_lines <= CBC_NOALLOC_MAX_LINES, else CBC_ERR_INVALID before any work; and
  * the lines' walks inside their frames may need at most CBC_NOALLOC_MAX_CHECKPOINTS
  * checkpoints (one per 8 columns of each walk), else the call draws nothing and
- * returns CBC_ERR_CAPACITY.  The call waits for `stream` and returns the call's full
- * status (CBC_OK, CBC_ERR_INDEX, CBC_ERR_CAPACITY, CBC_ERR_RANGE, ...; message in
- * cbc_last_error).  The first call on each device looks up the array's device
- * address with that device current; make that first call before any stream capture.
- * All calls share the one array and every call re-initialises it, so calls that
- * overlap on the GPU (unordered streams, or threads without ordering) race: issue
- * them one after another. */
+ * returns CBC_ERR_CAPACITY; n_frames must not exceed 2^31 - 1 (else CBC_ERR_INVALID).
+ * Every call looks up the array's device address for the current device and
+ * context (cudaGetSymbolAddress), so the address is never reused across contexts,
+ * e.g. after cudaDeviceReset.  The call synchronises `stream` (it reads the device
+ * status back) and returns the call's full status (CBC_OK, CBC_ERR_INDEX,
+ * CBC_ERR_CAPACITY, CBC_ERR_RANGE, ...; message in cbc_last_error).  All calls share
+ * the one array and every call re-initialises it, so calls that overlap on the GPU
+ * (unordered streams, or threads without ordering) race: issue them one after
+ * another. */
 CBC_API int cbc_draw_lines_f32_noalloc(float *out, int64_t n_frames, int64_t height,
                                        int64_t width, const float *lines, int64_t n_lines,
                                        const void *idxs, int32_t idx_bytes, float max_val,
@@ -306,15 +308,30 @@ CBC_API int cbc_squared_loss_step_sum_f32(const float *target, float *image, int
                                           size_t workspace_bytes, int64_t pair_capacity,
                                           int64_t checkpoint_capacity, void *stream);
 
-/* draw_lines into frames in page-locked host memory (cudaHostAlloc, or registered),
- * which the kernels address directly (NVLink-C2C on GB300): the lines are drawn into
+/* How the current device reaches the host memory at host_ptr: CBC_HOST_MAPPED
+ * (page-locked, through its device mapping), CBC_HOST_PAGEABLE (pageable memory,
+ * coherently through the host's page tables) or CBC_HOST_NONE (not at all: the
+ * frames must be copied).  No counterpart in the reference, whose host arrays are
+ * always drawn on the CPU. */
+#define CBC_HOST_NONE     0
+#define CBC_HOST_MAPPED   1
+#define CBC_HOST_PAGEABLE 2
+CBC_API int cbc_host_access(const void *host_ptr, int32_t *mode);
+
+/* draw_lines into frames in host memory that the kernels address directly over
+ * NVLink-C2C on GB300: page-locked memory (cudaHostAlloc, or registered) through its
+ * device mapping, or pageable memory (malloc, NumPy arrays) where the device reads
+ * and writes it coherently through the host's page tables
+ * (cudaDevAttrPageableMemoryAccess and cudaDevAttrPageableMemoryAccessUsesHostPageTables
+ * both set); host_out must be writable.  The lines are drawn into
  * `scratch` (n_frames * height * width device elements), which must hold the
  * overlap's identity on entry (-inf for CBC_MAX, -0.0 for CBC_SUM) unless `fill` is 1
  * (the call writes it first); then the pixels some line drew are combined into
  * host_out and `scratch` gets the identity back.  Only drawn pixels cross the link.
  * lines and idxs are device arrays; other arguments, the workspace and the errors as
- * cbc_draw_lines_f32 (an error leaves host_out untouched).  Pageable host memory is
- * rejected with CBC_ERR_INVALID.  Replaces the host-array path of the reference's
+ * cbc_draw_lines_f32 (an error leaves host_out untouched).  Host memory the device
+ * cannot address (pageable memory on other systems) is rejected with CBC_ERR_INVALID
+ * before anything runs.  Replaces the host-array path of the reference's
  * draw_lines (_src/functions.py:275-302, bresenham.cpp:313-331).  */
 CBC_API int cbc_draw_lines_host_f32(float *host_out, int64_t n_frames, int64_t height,
                                     int64_t width, const float *lines, int64_t n_lines,

@@ -45,3 +45,10 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return torch.device('cuda')
+
+
+@pytest.fixture(autouse=True)
+def _seeded_torch():
+    """every test starts from the same torch random state (CPU and CUDA generators)"""
+    import torch
+    torch.manual_seed(1234)

@@ -30,6 +30,20 @@ def test_exports_every_declared_symbol():
     assert set(_native.EXPORTS) <= names
 
 
+def test_noalloc_limits_match_the_header():
+    text = open(os.path.join(ROOT, 'include', 'cbc_draw_lines.h')).read()
+    defs = dict(re.findall(r'#define\s+(CBC_NOALLOC_MAX_\w+)\s+(\d+)', text))
+    assert int(defs['CBC_NOALLOC_MAX_LINES']) == _native.NOALLOC_MAX_LINES
+    assert int(defs['CBC_NOALLOC_MAX_CHECKPOINTS']) == _native.NOALLOC_MAX_CHECKPOINTS
+
+
+def test_noalloc_rejects_frame_counts_beyond_32_bits():
+    """rejected on the host, before any device call"""
+    lib = _native.lib()
+    rc = lib.cbc_draw_lines_f32_noalloc(None, 1 << 31, 1, 1, None, 1, None, 0, 1.0, 0, 0, None)
+    assert rc == _native.CBC_ERR_INVALID and 'n_frames' in _native.last_error()
+
+
 def test_version():
     assert b'sm_103a' in _native.lib().cbc_version()
 

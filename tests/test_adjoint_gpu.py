@@ -88,7 +88,8 @@ def test_gradient_matches_fp64_finite_differences(cuda, overlap):
     got32, _ = adjoint_gradient(lines, idxs, shape, target, kernel, overlap, max_val,
                                 torch.float32)
     per32, norm32 = relative_errors(got32, want)
-    assert norm32 <= 1e-3, (per32, norm32)
+    print(f"float32 adjoint, {overlap}: per parameter {per32:.3e}, 2-norm {norm32:.3e}")
+    assert norm32 <= RTOL, (per32, norm32)
 
 
 def torch_profile(kernel, x):

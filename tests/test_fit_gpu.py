@@ -39,7 +39,8 @@ def test_fused_squared_loss_gradient_matches_autograd(cuda, overlap):
     ls = workloads.fit_loop_stack(seed=9, F=2, H=200, W=180, per_frame=80)
     lines = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
     idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
-    target = torch.rand(ls.shape, device='cuda') * 50
+    target = torch.rand(ls.shape, device='cuda',
+                        generator=torch.Generator(device='cuda').manual_seed(9)) * 50
     p = lines.clone().requires_grad_(True)
     img = autograd.draw_lines_fn(p, idxs, shape=ls.shape, max_val=ls.max_val, kernel=ls.kernel,
                                  overlap=overlap)

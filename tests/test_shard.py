@@ -90,3 +90,46 @@ def test_two_cpu_ranks_render_their_frames(tmp_path):
     got = np.load(tmp_path / 'image.npy')
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
     assert np.isclose(np.load(tmp_path / 'loss.npy')[0], (ref ** 2).sum(), rtol=1e-12)
+
+
+def _fit_rank_main(rank, world, port, tmpdir):
+    """fit.shard_problem + fit.reduce_losses on CPU ranks: each rank's target frames,
+    lines and rebased indices, its loss (the oracle's render in place of the GPU fit)
+    and the summed loss"""
+    from cbclib_v2_gb300 import fit
+    os.environ.update(MASTER_ADDR='127.0.0.1', MASTER_PORT=str(port))
+    dist.init_process_group('gloo', rank=rank, world_size=world)
+    try:
+        ls = workloads.fit_loop_stack(seed=21, F=5, H=64, W=72, per_frame=20)
+        offs = ls.frame_offsets()
+        target = torch.from_numpy(np.random.default_rng(3).random(ls.shape))
+        sh, t, ln, ix = fit.shard_problem(target, torch.from_numpy(ls.lines), offs, rank, world)
+        assert t.shape[0] == sh.n_frames and ln.shape[0] == sh.n_lines
+        img = oracle.draw_lines(np.zeros(tuple(t.shape)), ln.numpy(), ix.numpy(), ls.max_val,
+                                ls.kernel, ls.overlap, 1)
+        mine = float(((img - t.numpy()) ** 2).sum())
+        total = fit.reduce_losses([mine, 2 * mine])
+        parts = [None] * world
+        dist.all_gather_object(parts, (sh.f0, sh.f1, sh.l0, sh.l1, ix.numpy()))
+        if rank == 0:
+            np.save(os.path.join(tmpdir, 'total.npy'), np.array(total))
+            np.save(os.path.join(tmpdir, 'parts.npy'), np.array(
+                [p[:4] for p in parts], dtype=np.int64))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_cpu_ranks_split_a_fit(tmp_path):
+    oracle._load()
+    mp.start_processes(_fit_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2,
+                       start_method='spawn', join=True)
+    ls = workloads.fit_loop_stack(seed=21, F=5, H=64, W=72, per_frame=20)
+    target = np.random.default_rng(3).random(ls.shape)
+    img = oracle.draw_lines(np.zeros(ls.shape), ls.lines, ls.idxs, ls.max_val, ls.kernel,
+                            ls.overlap, 1)
+    want = float(((img - target) ** 2).sum())
+    total = np.load(tmp_path / 'total.npy')
+    assert np.isclose(total[0], want, rtol=1e-12) and np.isclose(total[1], 2 * want, rtol=1e-12)
+    parts = np.load(tmp_path / 'parts.npy')
+    assert parts[0][0] == 0 and parts[-1][1] == ls.shape[0] and parts[0][1] == parts[1][0]
+    assert parts[0][2] == 0 and parts[-1][3] == ls.n_lines and parts[0][3] == parts[1][2]

@@ -98,7 +98,10 @@ def test_host_frames_index_error_leaves_frames(cuda):
     same(host, device_result(base, lines, idxs, 'biweight', 'sum', 1.0), 'sum')
 
 
-def test_pageable_frames_take_the_copying_path(cuda):
+def test_pageable_frames(cuda):
+    """NumPy arrays and unpinned tensors: drawn in place through the pageable mapping
+    where the device reads and writes pageable memory coherently (NVLink-C2C), copied
+    up and down otherwise; the result is the device path's either way"""
     rng = np.random.default_rng(25)
     F, H, W = 4, 30, 30
     lines = random_lines(rng, 12, H, W)
@@ -110,3 +113,24 @@ def test_pageable_frames_take_the_copying_path(cuda):
         want = device_result(torch.zeros((F, H, W), dtype=torch.float64), lines, idxs,
                              'parabolic', 'max', 1.0)
         assert torch.equal(torch.as_tensor(host), want)
+
+
+@pytest.mark.parametrize("overlap", ['sum', 'max'])
+def test_numpy_frames_in_place(cuda, overlap):
+    """a NumPy stack updated in place (the array object and its memory are kept), with
+    negative pixels, float32 and float64, against the device path"""
+    from cbclib_v2_gb300 import _native
+    rng = np.random.default_rng(26)
+    F, H, W = 7, 52, 61
+    lines = random_lines(rng, 200, H, W)
+    idxs = rng.integers(0, F, 200).astype(np.int32)
+    for dtype in (np.float32, np.float64):
+        base = (rng.random((F, H, W)) - 0.2).astype(dtype)
+        host = base.copy()
+        ptr = host.ctypes.data
+        out = draw_lines(host, lines.astype(dtype), idxs, 1.3, 'triangular', overlap)
+        assert out is host and host.ctypes.data == ptr
+        want = device_result(torch.from_numpy(base), lines, idxs, 'triangular', overlap, 1.3)
+        same(torch.from_numpy(host), want, overlap)
+    mode = _native.host_access(host.ctypes.data)
+    assert mode in (_native.HOST_PAGEABLE, _native.HOST_NONE)
