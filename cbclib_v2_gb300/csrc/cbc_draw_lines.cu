@@ -870,6 +870,42 @@ combine_host_kernel(T *__restrict__ host, T *__restrict__ scratch, long long n,
     }
 }
 
+/* how the current device reaches host memory at `p`: page-locked memory through its
+ * device mapping (CBC_HOST_MAPPED), pageable memory at its own address where the
+ * device accesses pageable memory coherently through the host's page tables
+ * (CBC_HOST_PAGEABLE), else not at all (CBC_HOST_NONE) */
+int host_address(void *p, void **dev)
+{
+    *dev = nullptr;
+    if (!p) return CBC_HOST_NONE;
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return CBC_HOST_NONE;
+    }
+    if (at.type == cudaMemoryTypeHost) {
+        void *m = nullptr;
+        if (cudaHostGetDevicePointer(&m, p, 0) == cudaSuccess && m) {
+            *dev = m;
+            return CBC_HOST_MAPPED;
+        }
+        cudaGetLastError();
+        return CBC_HOST_NONE;
+    }
+    if (at.type != cudaMemoryTypeUnregistered) return CBC_HOST_NONE;   /* device memory */
+    int d = 0, pageable = 0, host_tables = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) {
+        cudaGetLastError();
+        return CBC_HOST_NONE;
+    }
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, d);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, d);
+    if (!(pageable && host_tables)) return CBC_HOST_NONE;
+    *dev = p;
+    return CBC_HOST_PAGEABLE;
+}
+
 template <typename T>
 int draw_lines_host_impl(T *host_out, long long n_frames, long long H, long long W,
                          const T *lines, long long n_lines, const void *idxs, int idx_bytes,
@@ -887,22 +923,10 @@ int draw_lines_host_impl(T *host_out, long long n_frames, long long H, long long
     cudaGetDevice(&dev);
     T *dev_host = nullptr;
     if (n > 0) {
-        /* the device address of the host frames: the mapping of page-locked memory, or
-         * the host address itself where the device reads and writes pageable memory
-         * coherently through the host's page tables (NVLink-C2C systems) */
-        cudaError_t e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&dev_host),
-                                                 host_out, 0);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            int pageable = 0, host_tables = 0;
-            cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
-            cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
-                                   dev);
-            if (!(pageable && host_tables))
-                return fail(CBC_ERR_INVALID, "out is not host memory the device can address (" +
-                                                 std::string(cudaGetErrorString(e)) + ")");
-            dev_host = host_out;
-        }
+        void *p = nullptr;
+        if (host_address(host_out, &p) == CBC_HOST_NONE)
+            return fail(CBC_ERR_INVALID, "out is not host memory the device can address");
+        dev_host = static_cast<T *>(p);
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -960,20 +984,8 @@ int cbc_host_access(const void *host_ptr, int32_t *mode)
 {
     cbc::clear_error();
     if (!mode) return cbc::fail(CBC_ERR_INVALID, "null mode pointer");
-    *mode = CBC_HOST_NONE;
-    if (!host_ptr) return CBC_OK;
-    void *mapped = nullptr;
-    if (cudaHostGetDevicePointer(&mapped, const_cast<void *>(host_ptr), 0) == cudaSuccess) {
-        *mode = CBC_HOST_MAPPED;
-        return CBC_OK;
-    }
-    cudaGetLastError();
-    int dev = 0, pageable = 0, host_tables = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cbc::fail(CBC_ERR_CUDA, cudaGetErrorString(e));
-    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
-    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
-    if (pageable && host_tables) *mode = CBC_HOST_PAGEABLE;
+    void *dev_ptr = nullptr;
+    *mode = cbc::host_address(const_cast<void *>(host_ptr), &dev_ptr);
     return CBC_OK;
 }
 
