@@ -37,7 +37,6 @@ namespace cbc {
 
 template <typename T, int K, int MODE>
 struct AccumAct {
-    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
     T *out;
     T max_val;

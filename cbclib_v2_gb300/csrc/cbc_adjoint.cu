@@ -35,7 +35,6 @@ namespace cbc {
 /* max overlap: winner[p] = min over lines l with v_l(p) == image[p] > out0[p] */
 template <typename T, int K>
 struct WinnerAct {
-    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
     const T *image;
     const T *out0;       /* NULL: zeros */
@@ -186,7 +185,6 @@ __device__ __forceinline__ void pixel_term(const GradCoef<T> &c, T g, T X, T Y, 
 /* sum overlap: every drawn pixel (error <= 1) of every line gets its term */
 template <typename T, int K>
 struct BackwardAct {
-    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
     const T *lines;      /* (N, 5) parameters as given */
     const T *grad_out;   /* dL/dI, or NULL with image and target: L = sum((I - T)^2) */

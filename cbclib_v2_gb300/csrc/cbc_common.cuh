@@ -812,9 +812,8 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
  * condition) or when it leaves the frame.  The walks stay sequential per lane, as in
  * the reference, while the expensive per-pixel work runs on full warps.
  * act.item_begin(lane, slots) / act.item_end(lane, slots) bracket each warp item; an action
- * that reads the line geometry from the slot table sets kNeedsGeometry, one that needs
- * no error (and is handed every visited pixel) clears kNeedsError.  The forward,
- * the max-overlap winner pass and the adjoint are such actions. */
+ * that needs no error (and is handed every visited pixel) clears kNeedsError.  The
+ * forward, the max-overlap winner pass and the adjoint are such actions. */
 
 constexpr int kSegWarps = 4;
 constexpr int kSegMinBlocks = 6;   /* resident CTAs per SM the register budget targets */
@@ -844,7 +843,6 @@ struct SlotTable {
     int fast[32];        /* len and ww in the range of the reciprocal division */
     long long fbase[32]; /* frame * H * W                                      */
     int line[32];        /* line index, -1 for an empty slot                   */
-    T x0[32], y0[32], t0[32], t1[32], w[32];
 };
 
 /* a visited pixel waiting for evaluation: walk errors and frame coordinates, one
@@ -1013,13 +1011,6 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 S.fast[lane] = (r.flags & kFastDiv) ? 1 : 0;
                 S.fbase[lane] = (long long)r.frame * a.H * a.W;
                 S.line[lane] = ck.line;
-                if (Act::kNeedsGeometry) {
-                    S.x0[lane] = r.px;
-                    S.y0[lane] = r.py;
-                    S.t0[lane] = r.t0;
-                    S.t1[lane] = r.t1;
-                    S.w[lane] = r.w;
-                }
                 cols = true;
             }
         }

@@ -310,7 +310,6 @@ render_kernel(RenderArgs<T> a)
 
 template <typename T, int K, int OV>
 struct ForwardAct {
-    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
     T *out;
     T max_val;
@@ -336,7 +335,6 @@ struct ForwardAct {
  * line, which is the line sequential std::max keeps (bresenham.cpp:71) */
 template <int K>
 struct PackedMaxAct {
-    static constexpr bool kNeedsGeometry = false;
     static constexpr bool kNeedsError = true;
     unsigned long long *packed;
     float max_val;

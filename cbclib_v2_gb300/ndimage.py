@@ -18,7 +18,7 @@ from . import _native
 from . import device as _device
 
 __all__ = ['draw_lines', 'draw_lines_csr', 'accumulate_lines', 'Workspace', 'tuning',
-           'release_scratch']
+           'release_scratch', 'deferred_errors']
 
 _tls = threading.local()
 
@@ -250,14 +250,59 @@ class _on_current_device:
             self.ctx.__exit__(*exc)
 
 
+class _Deferred:
+    """the calls of one deferred_errors() block: a page-locked copy of each call's
+    device status and a function that runs the call again with room to spare"""
+
+    def __init__(self):
+        self.pending = []                # (status bytes, rerun, n_frames, device)
+
+    def finish(self) -> None:
+        lib = _native.lib()
+        for dev in {d for _, _, _, d in self.pending}:
+            torch.cuda.synchronize(dev)
+        pending, self.pending = self.pending, []
+        for buf, rerun, n_frames, _ in pending:
+            st = _native.Status()
+            lib.cbc_decode_status(buf.data_ptr(), st)
+            _raise_status(st, n_frames)
+            if st.has(_native.CBC_ERR_CAPACITY):
+                rerun()                  # it drew nothing: run it again, checked
+
+
+@contextlib.contextmanager
+def deferred_errors() -> Iterator[None]:
+    """Inside the block, draw_lines and draw_lines_csr calls on contiguous CUDA frames
+    return without waiting for the GPU: each call's device status (index and range
+    errors, and whether its walks fitted the workspace) is copied to page-locked host
+    memory asynchronously and all of them are checked when the block exits, after
+    waiting for the devices.  Back-to-back calls then queue on the stream while the
+    host prepares the next one.  On exit the first error raises (IndexError,
+    ValueError), as the call itself would have; a call that drew nothing because its
+    walks needed more room than the workspace held is run again then, in the order of
+    the block (overlaps combine in any order; float sums may differ in the last bits).
+    Host frames, other entry points and calls outside the block check as usual."""
+    prev = getattr(_tls, 'deferred', None)
+    d = _Deferred()
+    _tls.deferred = d
+    try:
+        yield
+    finally:
+        _tls.deferred = prev
+    d.finish()
+
+
 def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines: int,
-                        elem: int, tuning, size_fn=None) -> None:
+                        elem: int, tuning, size_fn=None, deferrable: bool = False) -> None:
     """Run `call(buf, capacity, ck_capacity, tref, stream)` with this thread's
     workspace, read the status, raise the reference's errors and repeat with a larger
     workspace when the call reports that its pairs or checkpoints did not fit.
     ``size_fn(F, H, W, n_lines, capacity, ck_capacity)`` sizes the workspace of calls
-    whose workspace starts with a draw_lines one (default: the draw_lines size)."""
+    whose workspace starts with a draw_lines one (default: the draw_lines size).  With
+    ``deferrable`` inside a deferred_errors() block the status is only copied
+    asynchronously (checked when the block exits)."""
     lib = _native.lib()
+    deferred = getattr(_tls, 'deferred', None) if deferrable else None
     with _on_current_device(dev):
         stream = _current_stream(dev)
         ws = _workspace_raw(dev, stream)
@@ -281,6 +326,16 @@ def _run_with_workspace(call, dev: torch.device, F: int, H: int, W: int, n_lines
             rc = call(buf, capacity, ck_capacity, tref, stream)
             if rc:
                 _raise_rc(rc)
+            if deferred is not None:
+                slot = torch.empty(int(lib.cbc_status_bytes()), dtype=torch.uint8,
+                                   pin_memory=True)
+                rc = lib.cbc_copy_status_async(buf.data_ptr(), slot.data_ptr(), stream)
+                if rc:
+                    _raise_rc(rc)
+                ws.capacity, ws.ck_capacity = capacity, ck_capacity
+                deferred.pending.append((slot, lambda: _run_with_workspace(
+                    call, dev, F, H, W, n_lines, elem, tuning, size_fn), F, dev))
+                return
             st = _native.Status()
             rc = lib.cbc_read_status(buf.data_ptr(), st, stream)
             if rc:
@@ -339,7 +394,7 @@ def _draw_lines_cuda(out: torch.Tensor, lines, idxs, max_val: float, kernel: int
                   max_val, kernel, overlap, buf.data_ptr(), buf.numel(), capacity, ck_capacity,
                   tref, stream)
 
-    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning)
+    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning, deferrable=work is out)
     if work is not out:
         out.copy_(work)
     return out
@@ -437,7 +492,7 @@ def draw_lines_csr(out: torch.Tensor, lines, frame_offsets, max_val: float = 1.0
         return fn(work.data_ptr(), F, H, W, ln.data_ptr(), n_lines, offs.data_ptr(), max_val, k,
                   ov, buf.data_ptr(), buf.numel(), capacity, ck_capacity, tref, stream)
 
-    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning)
+    _run_with_workspace(call, dev, F, H, W, n_lines, elem, tuning, deferrable=work is out)
     if work is not out:
         out.copy_(work)
     return out

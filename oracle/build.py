@@ -23,8 +23,12 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_reference() -> None:
+    """the reference's CPU module (compiled here), and its GPU module's sources staged
+    into oracle/_ref/cuda_src for a build on the GPU host (oracle/ref_cuda.py); both
+    are no-ops without the reference checkout"""
     script = os.path.join(HERE, "build_ref.sh")
     subprocess.run(["bash", script], check=True)
+    subprocess.run(["bash", os.path.join(HERE, "build_ref_cuda.sh"), "stage"], check=True)
 
 
 if __name__ == "__main__":
