@@ -505,7 +505,7 @@ def run_fit(args, world, rank, local):
                                  'speedup_vs_finite_difference_own_frame')}}), flush=True)
 
 
-def measure_ragged(steps: int, warmup: int, rank: int, local: int):
+def measure_ragged(steps: int, warmup: int, rank: int, local: int, frames: int = 256):
     """256 frames of 1024^2, lognormal(median 1,500, sigma 1) segments per frame clipped
     to [100, 20,000], triangular, sum: one graph replay of the autotuned CSR draw per
     step, against one eager draw_lines_csr call of the same stack and one public
@@ -513,7 +513,7 @@ def measure_ragged(steps: int, warmup: int, rank: int, local: int):
     import torch
     from cbclib_v2_gb300 import batch, ndimage, workloads
     torch.cuda.set_device(local)
-    ls = workloads.ragged_stack(seed=3000 + rank)
+    ls = workloads.ragged_stack(seed=3000 + rank, F=frames)
     offs = ls.frame_offsets()
     lines = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
     r = batch.RaggedRenderer(ls.shape, offs, max_val=ls.max_val, kernel=ls.kernel,
@@ -557,7 +557,8 @@ def measure_ragged(steps: int, warmup: int, rank: int, local: int):
 
 
 def run_ragged(args, world, rank, local):
-    r = measure_ragged(args.steps, args.warmup, rank, local)
+    r = measure_ragged(args.steps, args.warmup, rank, local,
+                       args.frames if args.frames_given else 256)
     if rank == 0:
         print(json.dumps({
             'metric': r['metric'], 'value': world * r['value'], 'unit': 'Mlines/s',

@@ -46,3 +46,57 @@ def module(build_if_missing: bool = True):
     spec.loader.exec_module(mod)
     _mod = mod
     return mod
+
+
+def compare_detector_stack(frames: int = 64, steps: int = 5) -> dict:
+    """The reference GPU module and this library on the detector-stack workload (64
+    frames of 2167x2070, Poisson(2,000) segments per frame, int32 frame indices,
+    max overlap): wall time per call with the GPU synchronised before and after (the
+    reference's call synchronises inside), best and median of `steps` calls into
+    zeroed frames, for the gaussian and the rectangular profile, and the pixels on
+    which the two results differ."""
+    import time
+    import numpy as np
+    import torch
+    from cbclib_v2_gb300 import draw_lines, workloads
+    mod = module()
+    if mod is None:
+        raise RuntimeError("reference CUDA module unavailable (oracle/build_ref_cuda.sh stage)")
+    ls = workloads.detector_stack(seed=1000, F=frames)
+    lines = torch.from_numpy(ls.lines.astype(np.float32)).cuda()
+    idxs = torch.from_numpy(ls.idxs.astype(np.int32)).cuda()
+
+    def timed(fn, out, k):
+        fn(out)
+        ts = []
+        for _ in range(k):
+            out.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn(out)
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return min(ts), sorted(ts)[len(ts) // 2]
+
+    res = {'workload': ls.name, 'lines': ls.n_lines, 'overlap': 'max'}
+    for kernel in ('gaussian', 'rectangular'):
+        ref = torch.zeros(ls.shape, device='cuda')
+        ours = torch.zeros(ls.shape, device='cuda')
+        r_best, r_med = timed(lambda o: mod.draw_lines(o, lines, idxs, 1.0, kernel, 'max'), ref,
+                              steps)
+        o_best, o_med = timed(lambda o: draw_lines(o, lines, idxs, 1.0, kernel, 'max'), ours,
+                              4 * steps)
+        res[kernel] = {'reference_ms_best': r_best, 'reference_ms_median': r_med,
+                       'this_library_ms_best': o_best, 'this_library_ms_median': o_med,
+                       'speedup_median': r_med / o_med,
+                       'pixels_differing': int((ref != ours).sum()),
+                       'pixels_drawn': int((ours != 0).sum()),
+                       'max_abs_difference': float((ref - ours).abs().max())}
+    return res
+
+
+if __name__ == '__main__':
+    import json
+    import sys
+    sys.path.insert(0, os.path.dirname(HERE))
+    print(json.dumps(compare_detector_stack()))
