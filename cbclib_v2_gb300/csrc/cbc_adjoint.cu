@@ -21,8 +21,10 @@
  * that recomputes them, and the gradient is then one streaming pass over the pixels
  * (dense_max_kernel) that adds each pixel's term to its winner's sums.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 #include <limits.h>
 #include <cmath>
 #include <string>
@@ -302,10 +304,14 @@ struct DenseArgs {
     double *partials;                   /* kSrcPacked: per-block sum of I (I - 2 T) over
                                            drawn pixels, or NULL */
     const DevStatus *st;                /* the forward's status (fatal: no gradient), or NULL */
+    int *err;                           /* status flags to mark a wait that gave up */
     unsigned long long *tasks;          /* task counter, zero at launch */
     long long n_px, n_chunks, n_items;
+    long long n_full;                   /* chunks of kChunk pixels wholly inside the frames */
     int n_lines, H, W, pitch;
     int vec;                            /* every base pointer is 16-byte aligned */
+    int tma;                            /* the tensor maps of the packed words and targets
+                                           are valid (kSrcPacked) */
 };
 
 /* 8 elements from p + p0: two or four 16-byte loads when aligned and in range */
@@ -403,30 +409,26 @@ constexpr int kDenseMaxBlocks = 2048;   /* persistent grid cap = loss partials *
 
 __device__ __forceinline__ int qslot(int i) { return i + (i >> 5); }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
+/* ---- staging of the packed pass ----
+ * A warp's chunk row is 32 chunks of 8 pixels: 2 KB of packed words and 1 KB of
+ * targets.  Where the 32 chunks are consecutive and whole (most rows: they are unless
+ * the row straddles a band edge or reaches the end of the frames) the row is fetched
+ * by the tensor memory accelerator: two cp.async.bulk.tensor copies issued by lane 0
+ * (boxes of 32 chunks x 64 B and 32 chunks x 32 B) that complete on the buffer's
+ * mbarrier, with the 64 B / 32 B swizzle so that each lane's 16-byte reads of its own
+ * chunk hit distinct banks.  Other rows are loaded by the lanes into the same swizzled
+ * layout.  Two buffers per warp: row k + 1 is in flight while row k is evaluated. */
+constexpr int kPkPieces = kChunk * 8 / 16;      /* 16-byte pieces of a chunk's packed words */
+constexpr int kTgPieces = kChunk * 4 / 16;      /* ... of its targets                       */
+constexpr int kPkRow = 32 * kChunk * 8;         /* bytes of a warp's row of packed words    */
+constexpr int kTgRow = 32 * kChunk * 4;         /* ... of targets                           */
+constexpr int kStageAlign = 1024;               /* the swizzle patterns repeat within this  */
+constexpr long long kWaitLimit = 1ll << 22;     /* bounded mbarrier waits (try_wait rounds) */
 
-__device__ __forceinline__ void cp_async_commit()
-{
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_1()
-{
-    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-}
-
-/* staging of the packed pass: per warp, two buffers of a chunk row's packed words and
- * targets, stored piece-major ([piece][lane] 16-byte pieces) so that each lane's
- * 16-byte reads of its own chunk are conflict-free */
-constexpr int kPkPieces = kChunk * 8 / 16;
-constexpr int kTgPieces = kChunk * 4 / 16;
 struct PackedStage {
-    uint4 pk[kDenseWarps][2][kPkPieces][32];
-    uint4 tg[kDenseWarps][2][kTgPieces][32];
+    unsigned char pk[kDenseWarps][2][kPkRow];
+    unsigned char tg[kDenseWarps][2][kTgRow];
+    unsigned long long bar[kDenseWarps][2];      /* mbarriers of the TMA buffers */
 };
 
 template <typename T>
@@ -446,55 +448,156 @@ __host__ __device__ constexpr size_t dense_stage_offset()
 template <typename T, int SRC>
 constexpr size_t dense_smem()
 {
-    return SRC == kSrcPacked && sizeof(T) == 4 ? dense_stage_offset<T>() + sizeof(PackedStage)
-                                               : sizeof(DenseQueueT<T>);
+    return SRC == kSrcPacked && sizeof(T) == 4
+               ? dense_stage_offset<T>() + kStageAlign + sizeof(PackedStage)
+               : sizeof(DenseQueueT<T>);
 }
 
-/* start the copy of chunk cc's packed words and targets into stage buffer buf (plain
- * loads for a chunk at the end of the frames or unaligned buffers) */
-__device__ __forceinline__ void stage_chunk(PackedStage &S, int wid, int lane, int buf,
-                                            long long cc, const DenseArgs<float> &a)
+__device__ __forceinline__ unsigned smem_addr(const void *p)
 {
-    if (cc < a.n_chunks) {
-        const long long p0 = cc * kChunk;
-        if (a.vec && p0 + kChunk <= a.n_px) {
-            const uint4 *gp = reinterpret_cast<const uint4 *>(a.packed + p0);
-            #pragma unroll
-            for (int j = 0; j < kPkPieces; j++) cp_async16(&S.pk[wid][buf][j][lane], gp + j);
-            const uint4 *gt = reinterpret_cast<const uint4 *>(a.target + p0);
-            #pragma unroll
-            for (int j = 0; j < kTgPieces; j++) cp_async16(&S.tg[wid][buf][j][lane], gt + j);
-        } else {
-            unsigned long long w[kChunk];
-            float t[kChunk];
-            #pragma unroll
-            for (int e = 0; e < kChunk; e++) {
-                const bool in = p0 + e < a.n_px;
-                w[e] = in ? a.packed[p0 + e] : 0ull;
-                t[e] = in ? a.target[p0 + e] : 0.0f;
-            }
-            uint4 q[kPkPieces], r[kTgPieces];
-            __builtin_memcpy(q, w, sizeof(w));
-            __builtin_memcpy(r, t, sizeof(t));
-            #pragma unroll
-            for (int j = 0; j < kPkPieces; j++) S.pk[wid][buf][j][lane] = q[j];
-            #pragma unroll
-            for (int j = 0; j < kTgPieces; j++) S.tg[wid][buf][j][lane] = r[j];
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+/* byte offset of 16-byte piece j of row r in a swizzled row buffer starting at shared
+ * address `base` (1024-aligned): rows of 64 B take the 64 B swizzle (piece index XOR
+ * address bits 7-8), rows of 32 B the 32 B swizzle (XOR address bit 7) */
+template <int ROW>
+__device__ __forceinline__ unsigned swz(unsigned base, int r, int j)
+{
+    const unsigned row = base + (unsigned)r * ROW;
+    const unsigned mask = ROW == 64 ? 3u : 1u;
+    return (unsigned)r * ROW + 16u * ((unsigned)j ^ ((row >> 7) & mask));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+/* lane 0: fetch box {0, c0} of both tensor maps into the buffer, completing on `bar` */
+__device__ __forceinline__ void tma_row(unsigned dst_pk, unsigned dst_tg, unsigned bar,
+                                        const CUtensorMap *tm_pk, const CUtensorMap *tm_tg,
+                                        long long c0)
+{
+    const int y = (int)c0;
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n"
+                 ::"r"(bar), "r"(kPkRow + kTgRow) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];\n"
+        ::"r"(dst_pk), "l"(reinterpret_cast<unsigned long long>(tm_pk)), "r"(0), "r"(y),
+          "r"(bar) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];\n"
+        ::"r"(dst_tg), "l"(reinterpret_cast<unsigned long long>(tm_tg)), "r"(0), "r"(y),
+          "r"(bar) : "memory");
+}
+
+/* start staging chunk row `cc` (this lane's chunk) into buffer buf: by TMA when the
+ * warp's 32 chunks are consecutive and whole, else by the lanes' own loads.  Returns
+ * true when a TMA copy is pending on the buffer's mbarrier. */
+__device__ __forceinline__ bool stage_row(unsigned char *pk, unsigned char *tg, unsigned bar,
+                                          int lane, long long cc, const DenseArgs<float> &a,
+                                          const CUtensorMap *tm_pk, const CUtensorMap *tm_tg)
+{
+    const long long c0 = __shfl_sync(0xffffffffu, cc, 0);
+    const bool tma = a.tma && __all_sync(0xffffffffu, cc == c0 + lane) && c0 + 32 <= a.n_full;
+    __syncwarp();                        /* every lane is done with the buffer's last row */
+    if (tma) {
+        if (lane == 0) tma_row(smem_addr(pk), smem_addr(tg), bar, tm_pk, tm_tg, c0);
+        return true;
+    }
+    unsigned long long w[kChunk];
+    float t[kChunk];
+    const long long p0 = cc * kChunk;
+    if (cc < a.n_chunks && a.vec && p0 + kChunk <= a.n_px) {
+        const uint4 *gp = reinterpret_cast<const uint4 *>(a.packed + p0);
+        const uint4 *gt = reinterpret_cast<const uint4 *>(a.target + p0);
+        uint4 q[kPkPieces], r[kTgPieces];
+        #pragma unroll
+        for (int j = 0; j < kPkPieces; j++) q[j] = gp[j];
+        #pragma unroll
+        for (int j = 0; j < kTgPieces; j++) r[j] = gt[j];
+        __builtin_memcpy(w, q, sizeof(w));
+        __builtin_memcpy(t, r, sizeof(t));
+    } else {
+        #pragma unroll
+        for (int e = 0; e < kChunk; e++) {
+            const bool in = cc < a.n_chunks && p0 + e < a.n_px;
+            w[e] = in ? a.packed[p0 + e] : 0ull;
+            t[e] = in ? a.target[p0 + e] : 0.0f;
         }
     }
-    cp_async_commit();
+    uint4 q[kPkPieces], r[kTgPieces];
+    __builtin_memcpy(q, w, sizeof(w));
+    __builtin_memcpy(r, t, sizeof(t));
+    const unsigned bp = smem_addr(pk), bt = smem_addr(tg);
+    #pragma unroll
+    for (int j = 0; j < kPkPieces; j++)
+        *reinterpret_cast<uint4 *>(pk + swz<64>(bp, lane, j)) = q[j];
+    #pragma unroll
+    for (int j = 0; j < kTgPieces; j++)
+        *reinterpret_cast<uint4 *>(tg + swz<32>(bt, lane, j)) = r[j];
+    return false;
 }
 
 /* Persistent: each warp takes tasks of 32 patches (one per lane) from a counter until
  * none are left, so the warps end together whatever the drawn density. */
 template <typename T, int K, int SRC>
 __global__ void __launch_bounds__(kDenseThreads, 3)
-dense_max_kernel(DenseArgs<T> a)
+dense_max_kernel(DenseArgs<T> a, const __grid_constant__ CUtensorMap tm_pk,
+                 const __grid_constant__ CUtensorMap tm_tg)
 {
     extern __shared__ __align__(16) unsigned char dense_smem_raw[];
     DenseQueueT<T> &Q = *reinterpret_cast<DenseQueueT<T> *>(dense_smem_raw);
-    PackedStage &S = *reinterpret_cast<PackedStage *>(dense_smem_raw + dense_stage_offset<T>());
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    /* the stage at the first 1024-aligned shared address after the queues */
+    const unsigned raw_sa = smem_addr(dense_smem_raw);
+    const unsigned stage_sa =
+        (raw_sa + (unsigned)dense_stage_offset<T>() + kStageAlign - 1) & ~(unsigned)(kStageAlign - 1);
+    PackedStage &S = *reinterpret_cast<PackedStage *>(dense_smem_raw + (stage_sa - raw_sa));
+    unsigned phases = 0u;      /* bit b: parity of buffer b's next TMA completion */
+    unsigned pending = 0u;     /* bit b: a TMA copy into buffer b is outstanding   */
+    bool failed = false;
+    if constexpr (SRC == kSrcPacked && sizeof(T) == 4) {
+        if (lane == 0) {
+            mbar_init(smem_addr(&S.bar[wid][0]));
+            mbar_init(smem_addr(&S.bar[wid][1]));
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        __syncwarp();
+    }
+    /* wait for buffer b's TMA copy, at most kWaitLimit rounds; a wait that gives up
+     * marks the status and stops the warp's work */
+    auto wait_buf = [&](int b) {
+        if (!((pending >> b) & 1u)) return;
+        bool ok = false;
+        const unsigned bar = smem_addr(&S.bar[wid][0]) + 8u * (unsigned)b;
+        for (long long i = 0; i < kWaitLimit && !ok; i++)
+            ok = mbar_try_wait(bar, (phases >> b) & 1u);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) {
+            if (lane == 0 && a.err) atomicOr(a.err, 1 << CBC_ERR_CUDA);
+            failed = true;
+        }
+        phases ^= 1u << b;
+        pending &= ~(1u << b);
+    };
     const bool grad = K != CBC_RECTANGULAR && !(a.st && (a.st->flags & kFatal));
     SlotPair<T> sp;
     sp.A.id = sp.B.id = -1;
@@ -508,7 +611,7 @@ dense_max_kernel(DenseArgs<T> a)
         long long task = 0;
         if (lane == 0) task = (long long)atomicAdd(a.tasks, 1ull);
         task = __shfl_sync(0xffffffffu, task, 0);
-        if (task >= n_tasks) break;
+        if (task >= n_tasks || failed) break;
         const long long it = task * 32 + lane;
         long long c = a.n_chunks;
         int x = 0, y = 0;
@@ -522,7 +625,9 @@ dense_max_kernel(DenseArgs<T> a)
             }
         }
         if constexpr (SRC == kSrcPacked && sizeof(T) == 4)
-            stage_chunk(S, wid, lane, 0, c, a);
+            if (stage_row(S.pk[wid][0], S.tg[wid][0], smem_addr(&S.bar[wid][0]), lane, c, a,
+                          &tm_pk, &tm_tg))
+                pending |= 1u;
         /* every lane of the warp takes part in each chunk row (the queue is shared) */
         #pragma unroll 1
         for (int k = 0; k < kPatchRows; k++, c += a.pitch) {
@@ -538,19 +643,27 @@ dense_max_kernel(DenseArgs<T> a)
                 gv[e] = T(0);
             }
             if constexpr (SRC == kSrcPacked && sizeof(T) == 4) {
+                const int buf = k & 1;
                 /* the next chunk row's copy goes out before this row is read */
-                if (k + 1 < kPatchRows) stage_chunk(S, wid, lane, (k + 1) & 1, c + a.pitch, a);
-                else cp_async_commit();
-                cp_async_wait_1();
+                if (k + 1 < kPatchRows &&
+                    stage_row(S.pk[wid][buf ^ 1], S.tg[wid][buf ^ 1],
+                              smem_addr(&S.bar[wid][buf ^ 1]), lane, c + a.pitch, a, &tm_pk,
+                              &tm_tg))
+                    pending |= 1u << (buf ^ 1);
+                wait_buf(buf);
+                if (failed) break;
+                __syncwarp();                /* the lanes' own stores of a loaded row */
                 if (live) {
-                    const int buf = k & 1;
                     unsigned long long wv[kChunk];
                     float tv[kChunk];
                     uint4 q[kPkPieces], r[kTgPieces];
+                    const unsigned bp = smem_addr(S.pk[wid][buf]), bt = smem_addr(S.tg[wid][buf]);
                     #pragma unroll
-                    for (int j = 0; j < kPkPieces; j++) q[j] = S.pk[wid][buf][j][lane];
+                    for (int j = 0; j < kPkPieces; j++)
+                        q[j] = *reinterpret_cast<const uint4 *>(S.pk[wid][buf] + swz<64>(bp, lane, j));
                     #pragma unroll
-                    for (int j = 0; j < kTgPieces; j++) r[j] = S.tg[wid][buf][j][lane];
+                    for (int j = 0; j < kTgPieces; j++)
+                        r[j] = *reinterpret_cast<const uint4 *>(S.tg[wid][buf] + swz<32>(bt, lane, j));
                     __builtin_memcpy(wv, q, sizeof(wv));
                     __builtin_memcpy(tv, r, sizeof(tv));
                     unsigned nz = 0;
@@ -642,6 +755,11 @@ dense_max_kernel(DenseArgs<T> a)
             }
             if (live) advance_px(x, y, kChunk, a.W, a.H);
         }
+    }
+    /* a warp that stopped on a failed wait still waits (bounded) for its other copy */
+    if constexpr (SRC == kSrcPacked && sizeof(T) == 4) {
+        wait_buf(0);
+        wait_buf(1);
     }
     sp.A.flush(a.gacc);
     sp.B.flush(a.gacc);
@@ -775,10 +893,62 @@ void dense_shape(DenseArgs<T> &a, long long n_frames, long long H, long long W)
     a.W = (int)W;
     a.n_px = n_frames * H * W;
     a.n_chunks = (a.n_px + kChunk - 1) / kChunk;
+    a.n_full = a.n_px / kChunk;
     a.pitch = dense_pitch(W);
     a.n_items = dense_items(a.n_px, W);
     a.vec = aligned16(a.packed) && aligned16(a.clear) && aligned16(a.winner) &&
             aligned16(a.grad_out) && aligned16(a.image) && aligned16(a.target);
+}
+
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link) */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled()
+{
+    static std::atomic<void *> fp{nullptr};
+    static std::atomic<int> tried{0};
+    void *p = fp.load(std::memory_order_acquire);
+    if (!p && !tried.load(std::memory_order_acquire)) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        fp.store(p, std::memory_order_release);
+        tried.store(1, std::memory_order_release);
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+}
+
+/* the tensor maps of the packed pass: the packed words and the targets as 2-D arrays
+ * of whole chunks (kChunk elements x n_full chunks), boxes of 32 chunks, swizzled 64 B
+ * and 32 B; false when they cannot be made (the pass then loads every row itself) */
+template <typename T>
+bool encode_packed_maps(const DenseArgs<T> &a, CUtensorMap *pk, CUtensorMap *tg)
+{
+    if (a.n_full < 32 || a.n_full > 0x7fffffffll || !a.packed || !a.target) return false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)kChunk, (cuuint64_t)a.n_full};
+    const cuuint32_t box[2] = {(cuuint32_t)kChunk, 32u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const cuuint64_t spk[1] = {(cuuint64_t)kChunk * 8};
+    const cuuint64_t stg[1] = {(cuuint64_t)kChunk * 4};
+    if (enc(pk, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2,
+            const_cast<unsigned long long *>(a.packed), dims, spk, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    if (enc(tg, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<T *>(a.target), dims, stg, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    return true;
 }
 
 /* the coefficient table of the lines, then the persistent pass: as many blocks as
@@ -797,6 +967,15 @@ cudaError_t launch_dense_k(const DenseArgs<T> &a, const T *lines, T max_val, cud
     }
     if (blocks) *blocks = 0;
     if (a.n_items < 1) return cudaSuccess;
+    CUtensorMap tm_pk, tm_tg;
+    DenseArgs<T> args = a;
+    args.tma = 0;
+    if constexpr (SRC == kSrcPacked && sizeof(T) == 4)
+        args.tma = args.vec && encode_packed_maps(a, &tm_pk, &tm_tg) ? 1 : 0;
+    if (!args.tma) {
+        memset(&tm_pk, 0, sizeof tm_pk);
+        memset(&tm_tg, 0, sizeof tm_tg);
+    }
     auto fn = dense_max_kernel<T, K, SRC>;
     constexpr size_t smem = dense_smem<T, SRC>();
     static std::atomic<int> grid_cache[64];
@@ -816,7 +995,7 @@ cudaError_t launch_dense_k(const DenseArgs<T> &a, const T *lines, T max_val, cud
     }
     const long long need = (a.n_items + kDenseThreads - 1) / kDenseThreads;
     const int grid = need < g ? (int)need : g;
-    fn<<<grid, kDenseThreads, smem, s>>>(a);
+    fn<<<grid, kDenseThreads, smem, s>>>(args, tm_pk, tm_tg);
     note_launches(1);
     if (blocks) *blocks = grid;
     return cudaGetLastError();
@@ -959,6 +1138,7 @@ int backward_impl(const T *grad_out, long long n_frames, long long H, long long 
         da.gacc = gacc;
         da.tasks = reinterpret_cast<unsigned long long *>(gacc + 5 * n_lines);
         da.st = walks ? st : nullptr;
+        da.err = &st->flags;
         da.n_lines = (int)n_lines;
         dense_shape(da, n_frames, H, W);
         if constexpr (sizeof(T) == 4) {
@@ -1042,6 +1222,7 @@ int loss_step_impl(const float *target, long long n_frames, long long H, long lo
         da.tasks = reinterpret_cast<unsigned long long *>(gacc + 5 * n_lines);
         da.partials = loss ? partials : nullptr;
         da.st = reinterpret_cast<const DevStatus *>(ws);   /* the forward's status block */
+        da.err = &reinterpret_cast<DevStatus *>(ws)->flags;
         da.n_lines = (int)n_lines;
         dense_shape(da, n_frames, H, W);
         e = launch_dense<float, kSrcPacked>(da, lines, max_val, kernel, s, &blocks);

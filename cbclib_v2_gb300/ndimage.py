@@ -194,6 +194,9 @@ def _as_device_idxs(idxs, n_lines: int, dev: torch.device) -> Optional[torch.Ten
 
 
 def _raise_status(st: _native.Status, n_frames: int):
+    if st.has(_native.CBC_ERR_CUDA):
+        raise RuntimeError("a device-side wait for an asynchronous copy gave up; the "
+                           "result of the call is incomplete")
     if st.has(_native.CBC_ERR_INDEX):
         raise IndexError(f"idxs range ({st.idx_min}, {st.idx_max}) is outside of "
                          f"(0, {n_frames})")

@@ -35,7 +35,9 @@ extern "C" {
 #define CBC_ERR_INVALID     1   /* bad argument: ValueError in the reference           */
 #define CBC_ERR_INDEX       2   /* frame index out of range: IndexError (bresenham.cpp:32-34) */
 #define CBC_ERR_CAPACITY    3   /* pair buffer too small; nothing was drawn, retry      */
-#define CBC_ERR_CUDA        4   /* CUDA runtime error: RuntimeError (cupy_array.hpp:18-24) */
+#define CBC_ERR_CUDA        4   /* CUDA runtime error: RuntimeError (cupy_array.hpp:18-24);
+                                   as a status flag: a device-side wait for an
+                                   asynchronous copy gave up (the result is incomplete) */
 #define CBC_ERR_RANGE       5   /* a line's walk is longer than CBC_MAX_WALK pixels     */
 #define CBC_ERR_TERM        6   /* accumulate_lines: a term index out of range: IndexError
                                    (bresenham.cpp:182-188); status flag only          */
