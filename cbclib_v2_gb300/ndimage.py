@@ -589,9 +589,19 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
     with _on_current_device(dev):
         if _native.host_access(host.data_ptr()) == _native.HOST_NONE:
             return False
-    ln = _as_device_lines(t, dev, host.dtype)
-    n = ln.shape[0]
-    ix = _as_device_idxs(idxs, n, dev)
+        # lines and indices in host memory the device reads are read in place (the
+        # kernels read each line once); others are copied to the device
+        ln = _host_readable(t.reshape(-1, 5) if t.is_contiguous() else None, host.dtype)
+        if ln is None:
+            ln = _as_device_lines(t, dev, host.dtype)
+        n = ln.shape[0]
+        ix = None
+        if idxs is not None:
+            ti = torch.as_tensor(idxs)
+            if ti.dtype in (torch.int32, torch.int64) and ti.numel() == n and ti.is_contiguous():
+                ix = _host_readable(ti.reshape(-1), ti.dtype)
+            if ix is None:
+                ix = _as_device_idxs(idxs, n, dev)
     if ix is None and n and F != 1 and F != n:
         raise ValueError(f"idxs has an incompatible size ({n} != {F})")
     elem = 4 if host.dtype == torch.float32 else 8
@@ -630,6 +640,15 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
         entry[1] = None                # unknown until the call has run
         _run_with_workspace(call, dev, F, H, W, n, elem, tuning)
     return True
+
+
+def _host_readable(t: Optional[torch.Tensor], dtype: torch.dtype) -> Optional[torch.Tensor]:
+    """`t` itself when it is a contiguous, non-empty CPU tensor of `dtype` in pageable
+    host memory that the current device reads at its own address (cbc_host_access,
+    NVLink-C2C systems), else None (page-locked memory is copied: that is one DMA)"""
+    if t is None or t.is_cuda or t.dtype != dtype or t.numel() == 0 or not t.is_contiguous():
+        return None
+    return t if _native.host_access(t.data_ptr()) == _native.HOST_PAGEABLE else None
 
 
 def _on_device(out, name: str, run):

@@ -330,7 +330,9 @@ CBC_API int cbc_host_access(const void *host_ptr, int32_t *mode);
  * overlap's identity on entry (-inf for CBC_MAX, -0.0 for CBC_SUM) unless `fill` is 1
  * (the call writes it first); then the pixels some line drew are combined into
  * host_out and `scratch` gets the identity back.  Only drawn pixels cross the link.
- * lines and idxs are device arrays; other arguments, the workspace and the errors as
+ * lines and idxs are device arrays or host memory the device reads (cbc_host_access:
+ * the kernels read each line and index once); other arguments, the workspace and the
+ * errors as
  * cbc_draw_lines_f32 (an error leaves host_out untouched).  Host memory the device
  * cannot address (pageable memory on other systems) is rejected with CBC_ERR_INVALID
  * before anything runs.  Replaces the host-array path of the reference's

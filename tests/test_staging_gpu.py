@@ -134,3 +134,23 @@ def test_numpy_frames_in_place(cuda, overlap):
         same(torch.from_numpy(host), want, overlap)
     mode = _native.host_access(host.ctypes.data)
     assert mode in (_native.HOST_PAGEABLE, _native.HOST_NONE)
+
+
+def test_numpy_lines_and_indices_read_in_place(cuda):
+    """NumPy frames, lines and int32/int64 indices (read by the kernels where they lie
+    on devices that reach pageable memory), float32 and float64, against the device
+    path; a float64 line array with float32 frames is converted first"""
+    rng = np.random.default_rng(27)
+    F, H, W = 5, 47, 66
+    lines = random_lines(rng, 150, H, W)
+    for dtype, idx_dtype in ((np.float32, np.int32), (np.float64, np.int64), (np.float32, np.int64)):
+        idxs = rng.integers(0, F, 150).astype(idx_dtype)
+        base = rng.random((F, H, W)).astype(dtype)
+        host = base.copy()
+        ln = np.ascontiguousarray(lines.astype(dtype))
+        draw_lines(host, ln, idxs, 1.1, 'biweight', 'max')
+        want = device_result(torch.from_numpy(base), lines, idxs, 'biweight', 'max', 1.1)
+        same(torch.from_numpy(host), want, 'max')
+    host = np.zeros((F, H, W), np.float32)
+    draw_lines(host, lines, rng.integers(0, F, 150), 1.1, 'biweight', 'max')   # float64 lines
+    assert host.any()
