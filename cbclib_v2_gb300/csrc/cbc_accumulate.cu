@@ -315,7 +315,7 @@ term_render2_kernel(Term2Args<T> a)
                     }
                     const int line = s_line[lo], col = j - s_pre[lo];
                     const LineRec<T> r = a.recs[line];
-                    const Checkpoint<T> ck = a.cks[r.ck_base + col / kSeg];
+                    const Checkpoint<T> ck = a.cks[r.ck_base + col / kCkCols];
                     if (ck.cx == INT_MIN) continue;
                     /* the walk from the checkpoint to the column: the position whose
                      * next move steps the long axis at walk index col */

@@ -51,8 +51,13 @@ struct alignas(16) LineRec {
 };
 
 /* the walk's exact iterator state at the first position whose walk index
- * (c - c0) * step_long reaches a multiple of kSeg (cx = INT_MIN: the walk ends first) */
+ * (c - c0) * step_long reaches a multiple of kCkCols (cx = INT_MIN: the walk ends
+ * first).  The lines render takes work items of kSeg columns, kCkCols / kSeg per
+ * checkpoint: an item that starts past its checkpoint walks there first. */
+constexpr int kCkCols = 16;
 constexpr int kSeg = 8;
+constexpr int kItemsPerCk = kCkCols / kSeg;
+static_assert(kCkCols % kSeg == 0, "render items tile the checkpoint spacing");
 
 template <typename T>
 struct Checkpoint {
@@ -463,7 +468,7 @@ prep_kernel(const T *__restrict__ lines, const void *__restrict__ idxs, long lon
                 if (cv.init(r, g)) {
                     r.ncols = cv.lmax - cv.lmin + 1;
                     r.c0 = cv.sa > 0 ? cv.lmin : cv.lmax;
-                    nck = (r.ncols + kSeg - 1) / kSeg;
+                    nck = (r.ncols + kCkCols - 1) / kCkCols;
                 } else {
                     r.flags = 0;        /* walk never enters the frame */
                 }
@@ -596,7 +601,7 @@ offsets_kernel(const int *__restrict__ counts, int *__restrict__ offsets,
     fillpos[b] = o32;
 }
 
-/* walk line i once and store the iterator state every kSeg walk columns inside the
+/* walk line i once and store the iterator state every kCkCols walk columns inside the
  * frame (LineIterator state: position and both errors) */
 template <typename T>
 __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> &cv,
@@ -608,7 +613,7 @@ __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> 
     wk.cy = r.y0;
     wk.te = r.te0;
     wk.ne = r.ne0;
-    const int nck = (r.ncols + kSeg - 1) / kSeg;
+    const int nck = (r.ncols + kCkCols - 1) / kCkCols;
     Checkpoint<T> *ck = cks + r.ck_base;
     int k = 0, next = 0;            /* next checkpoint: the first walk index >= next */
     const int x_end = r.x1, y_end = r.y1, c0 = r.c0, sa = cv.sa, ax = cv.a;
@@ -626,7 +631,7 @@ __device__ void write_checkpoints(const LineRec<T> &r, int i, const Coverage<T> 
             c.line = i;
             c.seg = k;
             ck[k++] = c;
-            next += kSeg;
+            next += kCkCols;
         }
         wk.step(wk.decide());
         if (++guard > 4LL * CBC_MAX_WALK + 64) {
@@ -794,10 +799,11 @@ __device__ __forceinline__ void global_combine_max<double>(double *addr, double 
 }
 
 /* ---- lines-strategy pixel enumeration ---------------------------------------------
- * Work items are (line, kSeg-column segment) pairs, i.e. walk checkpoints.  A warp
- * takes 32 of them from an atomic counter, one per lane, resumes every lane's walk
- * (bresenham.hpp:352-383 outer loop) from its checkpoint and handles the segment's
- * columns in kSeg rounds, one column per lane and round:
+ * Work items are (line, kSeg-column segment) pairs, kItemsPerCk per walk checkpoint.
+ * A warp takes 32 of them from an atomic counter, one per lane, resumes every lane's
+ * walk (bresenham.hpp:352-383 outer loop) from its checkpoint (walking past the columns
+ * before the segment) and handles the segment's columns in kSeg rounds, one column
+ * per lane and round:
  *   spans:   level k = 0, 1, 2, ... of all 32 columns at once: every lane advances
  *            the two span walks of its column (the inner loops, :369-380) by one step
  *            with the reference's float increments, and the visited in-frame pixels
@@ -880,7 +886,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SlotTable<T> &S = slot_s[warp];
     PixelRing<T> *rg = ring_s[warp];
-    const long long total = (long long)a.st->cks;
+    const long long total = (long long)a.st->cks * kItemsPerCk;
     const unsigned lanes_below = (1u << lane) - 1u;
     /* ring cursors, equal in every lane: ring 0 holds pixels within the segment's
      * extent along the line (0 <= te <= len^2, where the error is the normal term
@@ -979,7 +985,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
         T ts = T(0), ns = T(0), thr = T(0), len2 = T(0);
         bool cols = false;             /* columns of this item left to find */
         if (item < total) {
-            const Checkpoint<T> ck = a.cks[item];
+            const Checkpoint<T> ck = a.cks[item / kItemsPerCk];
             bool keep = true;
             if constexpr (FiltersLines<Act>::value) keep = act.keep_line(ck.line);
             if (ck.cx != INT_MIN && keep) {
@@ -994,7 +1000,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 y_end = r.y1;
                 c0 = r.c0;
                 sa = ax ? wk.sy : wk.sx;
-                lo = ck.seg * kSeg;
+                lo = ck.seg * kCkCols + (int)(item % kItemsPerCk) * kSeg;
                 hi = min(lo + kSeg - 1, r.ncols - 1);
                 s_hi = (ax ? a.W : a.H) - 1;
                 ts = ax ? r.t0 : r.t1;
@@ -1010,8 +1016,8 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 S.len2[lane] = r.len2;
                 S.fast[lane] = (r.flags & kFastDiv) ? 1 : 0;
                 S.fbase[lane] = (long long)r.frame * a.H * a.W;
-                S.line[lane] = ck.line;
-                cols = true;
+                cols = lo <= hi;                 /* a last item past the walk's end is empty */
+                S.line[lane] = cols ? ck.line : -1;
             }
         }
         act.item_begin(lane, S);

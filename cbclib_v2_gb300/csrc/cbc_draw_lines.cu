@@ -110,7 +110,7 @@ render_kernel(RenderArgs<T> a)
                 k_lo = max(k_lo, 0);
                 k_hi = min(k_hi, r.ncols - 1);
                 my_count = max(0, k_hi - k_lo + 1);
-                my_nseg = my_count > 0 ? k_hi / kSeg - k_lo / kSeg + 1 : 0;
+                my_nseg = my_count > 0 ? k_hi / kCkCols - k_lo / kCkCols + 1 : 0;
                 SlotParams<T> p;
                 p.ts = ax ? r.t0 : r.t1;              /* d te / d short */
                 p.ns = ax ? r.t1 : -r.t0;             /* d ne / d short: normal = (t1, -t0) */
@@ -159,7 +159,7 @@ render_kernel(RenderArgs<T> a)
         for (int e = threadIdx.x; e < total; e += blockDim.x) ent[e].c = kInvalidEntry;
         __syncthreads();
 
-        /* phase B: every (line, kSeg-column segment) resumes the walk (bresenham.hpp:
+        /* phase B: every (line, kCkCols-column segment) resumes the walk (bresenham.hpp:
          * 352-383 outer loop) from its checkpoint, one thread each, and records the
          * filled columns inside the tile */
         for (int it = threadIdx.x; it < nsegs; it += blockDim.x) {
@@ -168,10 +168,10 @@ render_kernel(RenderArgs<T> a)
             for (int bit = 16; bit > 0; bit >>= 1)
                 if (sl + bit < n && wsl[sl + bit].seg_base <= it) sl += bit;
             const WalkSlot<T> &w = wsl[sl];
-            const int sg = w.k_lo / kSeg + (it - w.seg_base);
+            const int sg = w.k_lo / kCkCols + (it - w.seg_base);
             const Checkpoint<T> ck = a.cks[w.ck_base + sg];
             if (ck.cx == INT_MIN) continue;
-            const int lo = max(sg * kSeg, w.k_lo), hi = min(sg * kSeg + kSeg - 1, w.k_hi);
+            const int lo = max(sg * kCkCols, w.k_lo), hi = min(sg * kCkCols + kCkCols - 1, w.k_hi);
             Walker<T> wk;
             wk.sx = w.sx;
             wk.sy = w.sy;

@@ -82,7 +82,7 @@ typedef struct cbc_status {
 } cbc_status;
 
 /* Bytes of device workspace a call with these sizes needs.  `pair_capacity` bounds
- * the (line, tile) pairs and `checkpoint_capacity` the walk checkpoints (one per 8
+ * the (line, tile) pairs and `checkpoint_capacity` the walk checkpoints (one per 16
  * columns of each line's walk inside its frame); when a call produces more of
  * either, it draws nothing, sets CBC_ERR_CAPACITY and reports both counts, so the
  * caller can grow the workspace and repeat the call. */
@@ -153,7 +153,7 @@ CBC_API int cbc_draw_lines_csr_f64(double *out, int64_t n_frames, int64_t height
  * Arguments and results are those of cbc_draw_lines_f32 (float32 only), with these
  * limits: n_lines <= CBC_NOALLOC_MAX_LINES, else CBC_ERR_INVALID before any work; and
  * the lines' walks inside their frames may need at most CBC_NOALLOC_MAX_CHECKPOINTS
- * checkpoints (one per 8 columns of each walk), else the call draws nothing and
+ * checkpoints (one per 16 columns of each walk), else the call draws nothing and
  * returns CBC_ERR_CAPACITY; n_frames must not exceed 2^31 - 1 (else CBC_ERR_INVALID).
  * Every call looks up the array's device address for the current device and
  * context (cudaGetSymbolAddress), so the address is never reused across contexts,

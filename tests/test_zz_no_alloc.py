@@ -118,16 +118,16 @@ def test_noalloc_index_widths_and_frame_per_line():
 
 
 def test_noalloc_checkpoint_limit_draws_nothing():
-    """walks needing more than CBC_NOALLOC_MAX_CHECKPOINTS checkpoints (one per 8
+    """walks needing more than CBC_NOALLOC_MAX_CHECKPOINTS checkpoints (one per 16
     columns): CBC_ERR_CAPACITY and the frames untouched; the next call is clean"""
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    W = 100000
-    n = 25                                   # 25 walks of ~12,400 checkpoints each
+    W = 200000
+    n = 25                                   # 25 walks of ~12,500 checkpoints each
     y = np.linspace(1.5, 6.5, n)
     lines = torch.tensor(np.c_[np.full(n, 10.0), y, np.full(n, W - 10.0), y, np.ones(n)],
                          dtype=torch.float32, device='cuda')
-    assert n * (W - 20) // 8 > _native.NOALLOC_MAX_CHECKPOINTS
+    assert n * (W - 20) // 16 > _native.NOALLOC_MAX_CHECKPOINTS
     out = torch.full((1, 8, W), 0.5, device='cuda')
     rc = _noalloc(out, lines, None, 1.0, 'rectangular', 'sum')
     assert rc == _native.CBC_ERR_CAPACITY and 'checkpoints' in _native.last_error()
