@@ -621,11 +621,14 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
             else:
                 _host_scratch[key] = entry           # most recently used last
         if entry is None:
-            entry = [torch.empty(F * H * W, dtype=host.dtype, device=dev), None]
+            # [buffer, overlap and dtype of its identity, elements holding that identity]
+            entry = [torch.empty(F * H * W, dtype=host.dtype, device=dev), None, 0]
             with _host_scratch_lock:
                 _host_scratch[key] = entry
         scratch = entry[0]
-        state = {'fill': int(entry[1] != tag)}
+        # a call over more elements than the identity covers (a smaller stack with
+        # another overlap came in between) fills its whole range again
+        state = {'fill': int(entry[1] != tag or entry[2] < F * H * W)}
 
         def call(buf, capacity, ck_capacity, tref, stream):
             rc = fn(host.data_ptr(), F, H, W, ln.data_ptr(), n,
@@ -633,6 +636,8 @@ def _draw_lines_staged(host: torch.Tensor, lines, idxs, max_val: float, kernel: 
                     max_val, kernel, overlap, scratch.data_ptr(), state['fill'], buf.data_ptr(),
                     buf.numel(), capacity, ck_capacity, tref, stream)
             if rc == 0:
+                if state['fill']:
+                    entry[2] = F * H * W
                 state['fill'] = 0      # the scratch is at the identity from here on
                 entry[1] = tag
             return rc

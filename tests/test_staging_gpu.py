@@ -73,6 +73,21 @@ def test_scratch_identity_kept_across_calls(cuda):
         host.copy_(ref.cpu())             # carry on from the same frames
 
 
+def test_scratch_identity_after_smaller_stacks(cuda):
+    """a large max stack, a small sum stack (which fills only its own part of the
+    cached scratch), then a middle-sized sum stack: the last call must fill the part
+    the small call left at the max identity"""
+    rng = np.random.default_rng(28)
+    for (F, H, W), overlap in (((6, 50, 60), 'max'), ((2, 30, 30), 'sum'),
+                               ((5, 44, 50), 'sum')):
+        lines = random_lines(rng, 80, H, W)
+        idxs = rng.integers(0, F, 80)
+        base = torch.rand((F, H, W))
+        host = base.clone().pin_memory()
+        draw_lines(host, lines, idxs, 1.2, 'parabolic', overlap)
+        same(host, device_result(base, lines, idxs, 'parabolic', overlap, 1.2), overlap)
+
+
 def test_host_frames_one_line_per_frame(cuda):
     rng = np.random.default_rng(23)
     F, H, W = 6, 40, 40
