@@ -865,6 +865,19 @@ struct PixelRing {
     unsigned char slot[kRing];     /* owner lane of each pixel */
 };
 
+/* an end-cap pixel (te < 0 or te > len^2) whose error is surely above 1: the error
+ * E = (ta^2 + ne^2) / (len^2 w^2) in exact arithmetic, with ta = max(-te, te - len^2),
+ * and the reference's float evaluation of E is within a few ulp of it, so
+ * ta^2 + ne^2 > len^2 w^2 (1 + 2^-13) in any rounding means E > 1: the pixel is not
+ * drawn and need not be queued.  Inside pixels are not tested: the span condition
+ * already bounds their error by 1. */
+template <typename T>
+__device__ __forceinline__ bool cap_far(T te, T ne, T len2, T lim)
+{
+    const T ta = fmax(-te, te - len2);
+    return ta * ta + ne * ne > lim;
+}
+
 /* actions that draw only some lines define keep_line(line) */
 template <class A, class = void> struct FiltersLines : std::false_type {};
 template <class A>
@@ -982,7 +995,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
 
         Walker<T> wk;
         int x_end = 0, y_end = 0, c0 = 0, sa = 1, lo = 0, hi = -1, ax = 0, s_hi = -1;
-        T ts = T(0), ns = T(0), thr = T(0), len2 = T(0);
+        T ts = T(0), ns = T(0), thr = T(0), len2 = T(0), cap_lim = T(0);
         bool cols = false;             /* columns of this item left to find */
         if (item < total) {
             const Checkpoint<T> ck = a.cks[item / kItemsPerCk];
@@ -1007,6 +1020,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 ns = ax ? r.t1 : -r.t0;
                 thr = r.ne_thr;
                 len2 = r.len2;
+                cap_lim = r.len2 * r.ww * T(1.0 + 0x1p-13);
                 EvalSlot<T> ev;
                 ev.len = r.len;
                 ev.rlen = r.rlen;
@@ -1056,8 +1070,9 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
             if (!col) cols = false;
 
             /* level 0: the column's centre pixel */
-            push(col && sc >= 0 && sc <= s_hi, te_c < T(0) || te_c > len2, te_c, ne_c,
-                 ax ? sc : c, ax ? c : sc);
+            const bool cap_c = te_c < T(0) || te_c > len2;
+            push(col && sc >= 0 && sc <= s_hi && !(cap_c && cap_far(te_c, ne_c, len2, cap_lim)),
+                 cap_c, te_c, ne_c, ax ? sc : c, ax ? c : sc);
             drain(31);
             /* levels 1, 2, ...: one step of the upward and the downward span walk */
             T tu = te_c, nu = ne_c, td = te_c, nd = ne_c;
@@ -1072,8 +1087,11 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 up = up && fabs(nu) < thr && su <= s_hi;
                 dn = dn && fabs(nd) < thr && sd >= 0;
                 if (!__any_sync(0xffffffffu, up || dn)) break;
-                push2(up && su >= 0, tu < T(0) || tu > len2, tu, nu, ax ? su : c, ax ? c : su,
-                      dn && sd <= s_hi, td < T(0) || td > len2, td, nd, ax ? sd : c, ax ? c : sd);
+                const bool cap_u = tu < T(0) || tu > len2, cap_d = td < T(0) || td > len2;
+                push2(up && su >= 0 && !(cap_u && cap_far(tu, nu, len2, cap_lim)), cap_u, tu, nu,
+                      ax ? su : c, ax ? c : su,
+                      dn && sd <= s_hi && !(cap_d && cap_far(td, nd, len2, cap_lim)), cap_d, td,
+                      nd, ax ? sd : c, ax ? c : sd);
                 drain(31);
             }
         }
