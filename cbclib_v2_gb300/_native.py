@@ -64,7 +64,8 @@ EXPORTS = ('cbc_draw_lines_workspace_size', 'cbc_draw_lines_f32', 'cbc_draw_line
            'cbc_squared_loss_step_sum_f32',
            'cbc_status_bytes', 'cbc_copy_status_async', 'cbc_decode_status',
            'cbc_adam_step_f32', 'cbc_draw_lines_host_f32', 'cbc_draw_lines_host_f64',
-           'cbc_host_access')
+           'cbc_host_access', 'cbc_draw_lines_3d_backward_workspace_size',
+           'cbc_draw_lines_3d_backward_f32', 'cbc_draw_lines_3d_backward_f64')
 
 HOST_NONE, HOST_MAPPED, HOST_PAGEABLE = 0, 1, 2
 
@@ -168,6 +169,13 @@ def _declare(lib):
     lib.cbc_version.restype = ctypes.c_char_p
     lib.cbc_host_access.argtypes = [p, ctypes.POINTER(i32)]
     lib.cbc_host_access.restype = ctypes.c_int
+    lib.cbc_draw_lines_3d_backward_workspace_size.argtypes = [i64, i64, i32]
+    lib.cbc_draw_lines_3d_backward_workspace_size.restype = ctypes.c_size_t
+    for sfx, real in (('f32', ctypes.c_float), ('f64', ctypes.c_double)):
+        f = getattr(lib, 'cbc_draw_lines_3d_backward_' + sfx)
+        f.argtypes = [p, i64, i64, i64, i64, p, i64, p, i32, real, i32, i32, p, p, p, p, p,
+                      ctypes.c_size_t, i64, p]
+        f.restype = ctypes.c_int
 
 
 def library_path() -> str:

@@ -1,6 +1,7 @@
 """Differentiable draw_lines: gradients of the drawn frames with respect to the line
-parameters (x0, y0, x1, y1, width), from the hand-written adjoint kernels
-(cbc_draw_lines_backward_*, csrc/cbc_adjoint.cu).
+parameters (x0, y0, x1, y1, width), or (x0, y0, z0, x1, y1, z1, width) for 3-D lines,
+from the hand-written adjoint kernels (cbc_draw_lines_backward_*, csrc/cbc_adjoint.cu;
+cbc_draw_lines_3d_backward_*, csrc/cbc_lines3d.cu).
 
 ``draw_lines_fn(lines, idxs, shape=..., max_val=..., kernel=..., overlap=...)`` returns
 new frames ``out0 + draw(lines)`` (``out0`` zeros unless given) and is differentiable
@@ -33,8 +34,11 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     if dtype not in (torch.float32, torch.float64):
         raise TypeError(f"frames must be float32 or float64, got {dtype}")
     ln = ndimage._as_device_lines(lines, dev, dtype)
-    if ln.shape[1] != 5:
-        raise ValueError("gradients are implemented for 2-D lines (N, 5)")
+    if ln.shape[1] == 7:
+        if grad_out is None or packed is not None or winner_known:
+            raise ValueError("3-D lines take the gradient of the volumes (grad_out)")
+        return _backward3(ln, idxs, max_val, k, ov, shape, dtype, dev, grad_out, image, out0,
+                          winner)
     n = ln.shape[0]
     ix = ndimage._as_device_idxs(idxs, n, dev)
     H, W = int(shape[-2]), int(shape[-1])
@@ -90,11 +94,49 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     raise RuntimeError("checkpoint capacity did not converge")
 
 
+def _backward3(ln, idxs, max_val: float, k: int, ov: int, shape, dtype, dev,
+               grad_out: torch.Tensor, image: Optional[torch.Tensor],
+               out0: Optional[torch.Tensor], winner: Optional[torch.Tensor]) -> torch.Tensor:
+    """cbc_draw_lines_3d_backward_*: the (N, 7) gradient for 3-D lines into volumes
+    (..., D, H, W)"""
+    if len(shape) < 3:
+        raise ValueError("3-D lines draw into volumes (..., D, H, W)")
+    D, H, W = (int(x) for x in shape[-3:])
+    F = math.prod(int(x) for x in shape[:-3])
+    n = ln.shape[0]
+    ix = ndimage._as_device_idxs(idxs, n, dev)
+    if ix is None and n and F != 1 and F != n:
+        raise ValueError(f"idxs has an incompatible size ({n} != {F})")
+    g = grad_out.to(dtype).contiguous()
+    img = None if image is None else image.to(dtype).contiguous()
+    o0 = None if out0 is None else out0.to(dtype).contiguous()
+    if ov == _native.OVERLAPS['max']:
+        if img is None:
+            raise ValueError("max overlap needs the forward image")
+        if winner is None:
+            winner = torch.empty(tuple(shape), dtype=torch.int32, device=dev)
+    grad = torch.empty((n, 7), dtype=dtype, device=dev)
+    lib = _native.lib()
+    elem = 4 if dtype == torch.float32 else 8
+    fn = getattr(lib, 'cbc_draw_lines_3d_backward_' + ('f32' if elem == 4 else 'f64'))
+    ndimage._run3(
+        lambda buf, ck, _t, stream: fn(
+            g.data_ptr(), F, D, H, W, ln.data_ptr(), n,
+            None if ix is None else ix.data_ptr(), 0 if ix is None else ix.element_size(),
+            max_val, k, ov, None if img is None else img.data_ptr(),
+            None if o0 is None else o0.data_ptr(), None if winner is None else winner.data_ptr(),
+            grad.data_ptr(), buf.data_ptr(), buf.numel(), ck, stream),
+        lambda ck, _t: lib.cbc_draw_lines_3d_backward_workspace_size(n, ck, elem),
+        dev, 'adjoint3d', F, n, columns=lambda: ndimage._columns3(ln, max(D, H, W)))
+    return grad
+
+
 def lines_backward(grad_out: torch.Tensor, lines: torch.Tensor, idxs: Optional[torch.Tensor],
                    max_val: float, kernel: str, overlap: str,
                    image: Optional[torch.Tensor] = None, out0: Optional[torch.Tensor] = None,
                    winner: Optional[torch.Tensor] = None) -> torch.Tensor:
-    """(N, 5) gradient of sum(grad_out * draw_lines(...)) with respect to ``lines``.
+    """(N, 5) gradient of sum(grad_out * draw_lines(...)) with respect to ``lines``
+    ((N, 7) for 3-D lines into volumes).
 
     ``grad_out`` has the frames' shape and dtype.  Max overlap also needs the forward
     result ``image`` (and ``out0`` if the frames were not zeros); ``winner`` (int32,
@@ -179,14 +221,15 @@ def draw_lines_fn(lines: torch.Tensor, idxs: Optional[torch.Tensor] = None, *,
                   shape: Optional[Sequence[int]] = None, out0: Optional[torch.Tensor] = None,
                   max_val: float = 1.0, kernel: str = 'rectangular',
                   overlap: str = 'sum') -> torch.Tensor:
-    """New frames ``out0 + draw_lines(lines)``, differentiable in ``lines`` (N, 5) and
-    ``out0``.  Give either ``shape`` (frames start at zero) or ``out0``."""
+    """New frames ``out0 + draw_lines(lines)``, differentiable in ``lines`` (N, 5), or
+    (N, 7) for 3-D lines into volumes, and ``out0``.  Give either ``shape`` (frames start
+    at zero) or ``out0``."""
     zero_base = out0 is None
     if out0 is None:
         if shape is None:
             raise ValueError("give shape or out0")
         out0 = torch.zeros(tuple(shape), dtype=lines.dtype, device=lines.device)
-    if lines.shape[-1] != 5:
+    if lines.shape[-1] not in (5, 7):
         raise RuntimeError(f"Invalid lines size ({lines.shape[-1]}) at axis {lines.ndim - 1}")
     ndimage._check_names(kernel, overlap)
     return DrawLinesFunction.apply(lines, out0, idxs, float(max_val), kernel, overlap, zero_base)

@@ -86,29 +86,7 @@ __device__ __forceinline__ GradCoef<T> make_grad_coef(T x0, T y0, T x1, T y1, T 
     c.y1 = y1;
     const T t0 = x1 - x0, t1 = y1 - y0;
     c.rmag = T(1) / (t0 * t0 + t1 * t1);
-    c.rw = T(1) / w;
-    const T rww = c.rw * c.rw;
-    switch (K) {
-    case CBC_BIWEIGHT:
-        c.k0 = T(-3.75) * max_val * rww;
-        c.k1 = -c.k0 * rww;
-        break;
-    case CBC_GAUSSIAN:
-        c.k0 = T(-9) * T(CBC_GAUSS_C) * max_val * rww;
-        c.k1 = T(-4.5) * rww;
-        break;
-    case CBC_PARABOLIC:
-        c.k0 = T(-1.5) * max_val * rww;
-        c.k1 = T(0);
-        break;
-    case CBC_RECTANGULAR:
-        c.k0 = c.k1 = T(0);
-        break;
-    default:
-        c.k0 = -max_val * c.rw;
-        c.k1 = T(0);
-        break;
-    }
+    kappa_consts<T, K>(w, max_val, c.k0, c.k1, c.rw);
     return c;
 }
 
@@ -122,25 +100,6 @@ grad_coef_kernel(const T *__restrict__ lines, long long n, T max_val,
     const T *ln = lines + i * 5;
     coef[i] = make_grad_coef<T, K>(ln[0], ln[1], ln[2], ln[3], ln[4], max_val);
 }
-
-template <typename T, int K>
-__device__ __forceinline__ T kappa_d2(T d2, T k0, T k1)
-{
-    switch (K) {
-    case CBC_BIWEIGHT:  return k0 + k1 * d2;
-    case CBC_GAUSSIAN:  return k0 * exp(k1 * d2);
-    case CBC_PARABOLIC: return k0;
-    case CBC_RECTANGULAR: return T(0);
-    default: {
-        const T d = sqrt(d2);
-        return d > T(0) ? k0 / d : T(0);
-    }
-    }
-}
-
-template <typename T> __device__ __forceinline__ T fma_rn(T a, T b, T c);
-template <> __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-template <> __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 /* g * dv/dtheta of one line at pixel (X, Y): v[0..4] for x0, y0, x1, y1, w.
  * The geometry is taken relative to the pixel from the end points as given: a pixel

@@ -1139,6 +1139,70 @@ unsigned resident_grid(F kernel, int threads)
     return (unsigned)g;
 }
 
+/* ---- adjoint helpers shared by the 2-D and 3-D gradients ----------------------------
+ * A line draws v = max_val K(d / w), d the distance from the pixel (voxel) centre to the
+ * segment.  With q the nearest point of the segment and s its position along it, the
+ * envelope theorem gives dv/dp0 = kappa (1 - s)(q - P), dv/dp1 = kappa s (q - P) and
+ * dv/dw = -kappa d^2 / w with kappa = max_val K'(d / w) / (w d), which is finite at
+ * d = 0 for the smooth profiles.  kappa as a function of d^2: k0 + k1 d^2 (biweight,
+ * parabolic with k1 = 0), k0 exp(k1 d^2) (gaussian), k0 / d (triangular, 0 at d = 0),
+ * 0 (rectangular); rw = 1 / w.  Profiles of include.hpp:447-468. */
+template <typename T, int K>
+__device__ __forceinline__ void kappa_consts(T w, T max_val, T &k0, T &k1, T &rw)
+{
+    rw = T(1) / w;
+    const T rww = rw * rw;
+    switch (K) {
+    case CBC_BIWEIGHT:
+        k0 = T(-3.75) * max_val * rww;
+        k1 = -k0 * rww;
+        break;
+    case CBC_GAUSSIAN:
+        k0 = T(-9) * T(CBC_GAUSS_C) * max_val * rww;
+        k1 = T(-4.5) * rww;
+        break;
+    case CBC_PARABOLIC:
+        k0 = T(-1.5) * max_val * rww;
+        k1 = T(0);
+        break;
+    case CBC_RECTANGULAR:
+        k0 = k1 = T(0);
+        break;
+    default:
+        k0 = -max_val * rw;
+        k1 = T(0);
+        break;
+    }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ T kappa_d2(T d2, T k0, T k1)
+{
+    switch (K) {
+    case CBC_BIWEIGHT:  return k0 + k1 * d2;
+    case CBC_GAUSSIAN:  return k0 * exp(k1 * d2);
+    case CBC_PARABOLIC: return k0;
+    case CBC_RECTANGULAR: return T(0);
+    default: {
+        const T d = sqrt(d2);
+        return d > T(0) ? k0 / d : T(0);
+    }
+    }
+}
+
+template <typename T> __device__ __forceinline__ T fma_rn(T a, T b, T c);
+template <> __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <> __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+/* p q - r s within 2 ulp: the product r s and its FMA error term (Kahan's difference
+ * of products) */
+template <typename T>
+__device__ __forceinline__ T diff_of_products(T p, T q, T r, T s)
+{
+    const T rs = r * s;
+    return fma_rn(p, q, -rs) + fma_rn(-r, s, rs);
+}
+
 /* host-side error reporting, defined in cbc_draw_lines.cu */
 int fail(int code, const std::string &msg);
 /* offsets of the line records and walk checkpoints in a draw_lines workspace laid out

@@ -30,6 +30,7 @@
 #include <stdint.h>
 #include <limits.h>
 #include <string>
+#include <type_traits>
 
 #include "cbc_accumulate.cuh"
 
@@ -413,6 +414,11 @@ struct Emit3 {
     }
 };
 
+/* emitters that need the voxel's coordinates (the adjoint) define voxel(...) */
+template <class EM, class = void> struct TakesCoords : std::false_type {};
+template <class EM>
+struct TakesCoords<EM, std::void_t<decltype(&EM::voxel)>> : std::true_type {};
+
 /* a visited voxel with normal error nf: inside the volume and with error <= 1, the emit */
 template <typename T, class EM>
 __device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, T nf, const Vol &v,
@@ -424,7 +430,8 @@ __device__ __forceinline__ void visit(const Rec3<T> &r, const It3<T> &it, T nf, 
     const T E = error(r, it, nf);
     if (!(E <= T(1))) return;
     const long long vox = ((long long)it.cur[2] * v.H + it.cur[1]) * v.W + it.cur[0];
-    emit(fbase, vox, line, E);
+    if constexpr (TakesCoords<EM>::value) emit.voxel(fbase, vox, line, E, it.cur);
+    else emit(fbase, vox, line, E);
 }
 
 template <typename T>
@@ -1074,6 +1081,346 @@ int accumulate3_impl(T *out, long long n_frames, long long D, long long H, long 
                    n_terms);
 }
 
+/* ---- adjoint: gradient of draw_lines with respect to the 3-D line parameters ----
+ * (x0, y0, z0, x1, y1, z1, w), from dL/dI, over exactly the voxel visits the forward
+ * makes (no counterpart in the reference).  The visits are replayed by the same
+ * (column, quadrant) items as render3_kernel; a voxel the reference visits twice adds
+ * its term twice under sum overlap, as the forward adds its value twice.  Max overlap:
+ * a winner pass first records each voxel's winner (the smallest line whose exact
+ * value equals the forward's result and exceeds the volume before drawing, the line
+ * sequential std::max keeps), then the gradient pass gives a voxel's term to its
+ * winner once: the winner's first visit claims the voxel by swapping its entry to
+ * -2 - line, and a last pass puts the winners back. */
+
+/* per-line constants of the voxel terms: end points as given, rmag = 1 / |p1 - p0|^2,
+ * the profile's kappa constants and rw = 1 / w */
+template <typename T>
+struct GradCoef3 {
+    T p0[3], p1[3];
+    T rmag, k0, k1, rw;
+};
+
+template <typename T, int K>
+__device__ __forceinline__ GradCoef3<T> make_grad_coef3(const T *ln, T max_val)
+{
+    GradCoef3<T> c;
+    T mag = T(0);
+    #pragma unroll
+    for (int i = 0; i < 3; i++) {
+        c.p0[i] = ln[i];
+        c.p1[i] = ln[3 + i];
+        const T t = c.p1[i] - c.p0[i];
+        mag += t * t;
+    }
+    c.rmag = T(1) / mag;
+    kappa_consts<T, K>(ln[6], max_val, c.k0, c.k1, c.rw);
+    return c;
+}
+
+/* g * dv/dtheta of one line at voxel P = (X, Y, Z): v[0..6] for x0, y0, z0, x1, y1, z1,
+ * w.  With a = p0 - P and e = p1 - P (exact: an integer minus an end point) and
+ * t = e - a, s = -(a . t) / |t|^2; beyond an end q is that end point, inside
+ * q - P = (t x c) / |t|^2 with c = a x e (each component a difference of products with
+ * its FMA error term), so q - P carries no cancellation error, and d^2 = |c|^2 / |t|^2. */
+template <typename T, int K>
+__device__ __forceinline__ void voxel_term(const GradCoef3<T> &c, T g, const int32_t *P,
+                                           T (&v)[7])
+{
+    T a[3], e[3], t[3];
+    #pragma unroll
+    for (int i = 0; i < 3; i++) {
+        a[i] = c.p0[i] - (T)P[i];
+        e[i] = c.p1[i] - (T)P[i];
+        t[i] = e[i] - a[i];
+    }
+    T s = -(a[0] * t[0] + a[1] * t[1] + a[2] * t[2]) * c.rmag;
+    T dv[3], d2;
+    if (s <= T(0)) {
+        s = T(0);
+        #pragma unroll
+        for (int i = 0; i < 3; i++) dv[i] = a[i];
+        d2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    } else if (s >= T(1)) {
+        s = T(1);
+        #pragma unroll
+        for (int i = 0; i < 3; i++) dv[i] = e[i];
+        d2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+    } else {
+        const T cx = diff_of_products(a[1], e[2], a[2], e[1]);
+        const T cy = diff_of_products(a[2], e[0], a[0], e[2]);
+        const T cz = diff_of_products(a[0], e[1], a[1], e[0]);
+        dv[0] = (t[1] * cz - t[2] * cy) * c.rmag;
+        dv[1] = (t[2] * cx - t[0] * cz) * c.rmag;
+        dv[2] = (t[0] * cy - t[1] * cx) * c.rmag;
+        d2 = (cx * cx + cy * cy + cz * cz) * c.rmag;
+    }
+    const T G = g * kappa_d2<T, K>(d2, c.k0, c.k1);
+    const T gb = G * s, ga = G - gb;
+    #pragma unroll
+    for (int i = 0; i < 3; i++) {
+        v[i] = ga * dv[i];
+        v[3 + i] = gb * dv[i];
+    }
+    v[6] = -G * d2 * c.rw;
+}
+
+/* winner pass: every drawn voxel whose value is the forward's result and above the
+ * volume before drawing offers its line; the smallest index stays */
+template <typename T, int K>
+struct WinnerEmit3 {
+    const T *image;
+    const T *out0;       /* NULL: zeros */
+    int *winner;
+    T max_val;
+    __device__ __forceinline__ void operator()(long long fbase, long long vox, int line,
+                                               T E) const {
+        using A = Ar<T>;
+        const long long at = fbase + vox;
+        const T v = A::mul(max_val, A::template profile<K>(A::sqrt(E)));
+        const T img = image[at];
+        const T o = out0 ? out0[at] : T(0);
+        if (v == img && o < img) atomicMin(winner + at, line);
+    }
+};
+
+/* gradient pass: the item's terms summed in registers (acc) */
+template <typename T, int K, bool MAX>
+struct AdjEmit3 {
+    const T *grad_out;
+    int *winner;         /* MAX: the winner map, claimed entry by entry */
+    GradCoef3<T> coef;   /* the current item's line */
+    mutable T acc[7];
+    __device__ __forceinline__ void voxel(long long fbase, long long vox, int line, T,
+                                          const int32_t *cur) const {
+        const long long at = fbase + vox;
+        if constexpr (MAX) {
+            if (winner[at] != line) return;
+            if (atomicCAS(winner + at, line, -2 - line) != line) return;   /* counted once */
+        }
+        const T g = grad_out[at];
+        if (g == T(0)) return;
+        T v[7];
+        voxel_term<T, K>(coef, g, cur, v);
+        #pragma unroll
+        for (int k = 0; k < 7; k++) acc[k] += v[k];
+    }
+};
+
+template <typename T>
+struct Adj3Args {
+    const Rec3<T> *recs;
+    const Ck3<T> *cks;
+    const T *lines;      /* (N, 7) as given */
+    Vol v;
+    DevStatus *st;
+    double *gacc;        /* (N, 7) */
+    T max_val;
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kThreads)
+winner3_kernel(Adj3Args<T> a, WinnerEmit3<T, K> emit)
+{
+    if (a.st->flags & kFatal) return;
+    const long long ncks = (long long)a.st->cks, total = 4 * ncks;
+    for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(item / ncks);
+        const Ck3<T> ck = a.cks[item - (long long)q * ncks];
+        if (ck.cur[0] == INT_MIN) continue;
+        const Rec3<T> r = a.recs[ck.line];
+        const long long fbase = (long long)r.frame * a.v.D * a.v.H * a.v.W;
+        draw_quadrants(r, column_iter(r, ck), q, q + 1, a.v, fbase, ck.line, emit, a.st);
+    }
+}
+
+/* one thread per (column, quadrant) as render3_kernel, in warp-uniform steps so that
+ * the lanes holding the same line (neighbouring columns) sum their terms by shuffles
+ * and one of them adds them to the line's double accumulators */
+template <typename T, int K, bool MAX>
+__global__ void __launch_bounds__(kThreads)
+adjoint3_kernel(Adj3Args<T> a, const T *grad_out, int *winner)
+{
+    if (a.st->flags & kFatal) return;
+    const int lane = threadIdx.x & 31;
+    const long long ncks = (long long)a.st->cks, total = 4 * ncks;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+         base < total; base += stride) {
+        const long long item = base + lane;
+        AdjEmit3<T, K, MAX> em;
+        em.grad_out = grad_out;
+        em.winner = winner;
+        #pragma unroll
+        for (int k = 0; k < 7; k++) em.acc[k] = T(0);
+        int key = -1;
+        if (item < total) {
+            const int q = (int)(item / ncks);
+            const Ck3<T> ck = a.cks[item - (long long)q * ncks];
+            if (ck.cur[0] != INT_MIN) {
+                const Rec3<T> r = a.recs[ck.line];
+                key = ck.line;
+                em.coef = make_grad_coef3<T, K>(a.lines + (size_t)ck.line * 7, a.max_val);
+                const long long fbase = (long long)r.frame * a.v.D * a.v.H * a.v.W;
+                draw_quadrants(r, column_iter(r, ck), q, q + 1, a.v, fbase, ck.line, em, a.st);
+            }
+        }
+        __syncwarp();
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        const int most = __reduce_max_sync(0xffffffffu, key >= 0 ? __popc(peers) : 0);
+        T sum[7];
+        #pragma unroll
+        for (int k = 0; k < 7; k++) sum[k] = em.acc[k];
+        unsigned rest = peers & (peers - 1u);            /* the group without its leader */
+        for (int i = 1; i < most; i++) {
+            const int src = rest ? __ffs(rest) - 1 : lane;
+            const bool take = lane == leader && rest != 0u;
+            #pragma unroll
+            for (int k = 0; k < 7; k++) {
+                const T o = __shfl_sync(0xffffffffu, em.acc[k], src);
+                if (take) sum[k] += o;
+            }
+            rest &= rest - 1u;
+        }
+        if (key >= 0 && lane == leader) {
+            #pragma unroll
+            for (int k = 0; k < 7; k++)
+                if (sum[k] != T(0)) atomicAdd(a.gacc + (size_t)key * 7 + k, (double)sum[k]);
+        }
+    }
+}
+
+/* the double sums into grad_lines; claimed winners (-2 - line) back to their lines */
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+adjoint3_finish_kernel(const double *__restrict__ gacc, T *__restrict__ grad, long long n7,
+                       int *__restrict__ winner, long long n_vox)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n7; i += stride)
+        grad[i] = (T)gacc[i];
+    if (!winner) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_vox; i += stride) {
+        const int w = winner[i];
+        if (w < -1) winner[i] = -2 - w;
+    }
+}
+
+/* workspace of the 3-D adjoint: the draw layout, then the (N, 7) double sums */
+inline size_t adjoint3_gacc_offset(long long n_lines, long long ck_capacity, size_t elem)
+{
+    return layout3(n_lines, 0, ck_capacity, 0, elem).total;
+}
+
+inline size_t adjoint3_workspace(long long n_lines, long long ck_capacity, size_t elem)
+{
+    return adjoint3_gacc_offset(n_lines, ck_capacity, elem) +
+           ((sizeof(double) * 7 * (size_t)n_lines + 255) / 256) * 256;
+}
+
+template <typename T, int K>
+cudaError_t launch_adjoint3(const Adj3Args<T> &a, int overlap, const T *grad_out,
+                            const T *image, const T *out0, int *winner, cudaStream_t s)
+{
+    if (overlap == CBC_MAX) {
+        WinnerEmit3<T, K> we{image, out0, winner, a.max_val};
+        winner3_kernel<T, K><<<resident_grid(winner3_kernel<T, K>, kThreads), kThreads, 0, s>>>(
+            a, we);
+        adjoint3_kernel<T, K, true>
+            <<<resident_grid(adjoint3_kernel<T, K, true>, kThreads), kThreads, 0, s>>>(
+                a, grad_out, winner);
+        note_launches(2);
+    } else {
+        adjoint3_kernel<T, K, false>
+            <<<resident_grid(adjoint3_kernel<T, K, false>, kThreads), kThreads, 0, s>>>(
+                a, grad_out, nullptr);
+        note_launches(1);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+int backward3_impl(const T *grad_out, long long n_frames, long long D, long long H, long long W,
+                   const T *lines, long long n_lines, const void *idxs, int idx_bytes,
+                   T max_val, int kernel, int overlap, const T *image, const T *out0,
+                   int *winner, T *grad_lines, void *workspace, size_t ws_bytes,
+                   long long ck_capacity, void *stream)
+{
+    clear_error();
+    if (n_frames < 0 || D < 0 || H < 0 || W < 0 || n_lines < 0)
+        return fail(CBC_ERR_INVALID, "negative size");
+    if (kernel < CBC_BIWEIGHT || kernel > CBC_TRIANGULAR)
+        return fail(CBC_ERR_INVALID, "kernel is missing");
+    if (overlap != CBC_SUM && overlap != CBC_MAX) return fail(CBC_ERR_INVALID, "Invalid overlap keyword");
+    if (idxs && idx_bytes != 4 && idx_bytes != 8) return fail(CBC_ERR_INVALID, "idx_bytes must be 4 or 8");
+    if (!idxs && n_lines > 0 && n_frames != 1 && n_frames != n_lines)
+        return fail(CBC_ERR_INVALID, "idxs has an incompatible size (" + std::to_string(n_lines) +
+                                         " != " + std::to_string(n_frames) + ")");
+    if (n_lines > INT_MAX) return fail(CBC_ERR_INVALID, "too many lines");
+    if (D * H * W > INT_MAX) return fail(CBC_ERR_INVALID, "volumes larger than 2^31 voxels");
+    if (ck_capacity < 0 || ck_capacity > INT_MAX)
+        return fail(CBC_ERR_INVALID, "checkpoint_capacity out of range");
+    const long long voxels = n_frames * D * H * W;
+    if (n_lines > 0 && (!lines || !grad_lines)) return fail(CBC_ERR_INVALID, "null pointer");
+    if (n_lines > 0 && voxels > 0 && !grad_out) return fail(CBC_ERR_INVALID, "null pointer");
+    if (overlap == CBC_MAX && n_lines > 0 && voxels > 0 && (!image || !winner))
+        return fail(CBC_ERR_INVALID, "max overlap needs the forward image and a winner buffer");
+    const Layout3 L = layout3(n_lines, 0, ck_capacity, 0, sizeof(T));
+    const size_t need = adjoint3_workspace(n_lines, ck_capacity, sizeof(T));
+    if (!workspace || ws_bytes < need)
+        return fail(CBC_ERR_INVALID, "workspace too small (" + std::to_string(ws_bytes) + " < " +
+                                         std::to_string(need) + ")");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char *ws = static_cast<unsigned char *>(workspace);
+    DevStatus *st = reinterpret_cast<DevStatus *>(ws + L.status);
+    double *gacc = reinterpret_cast<double *>(ws + adjoint3_gacc_offset(n_lines, ck_capacity,
+                                                                        sizeof(T)));
+    init_status_kernel<<<1, 1, 0, s>>>(st, CBC_STRATEGY_LINES);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && n_lines > 0)
+        e = cudaMemsetAsync(gacc, 0, sizeof(double) * 7 * (size_t)n_lines, s);
+    const bool maxw = overlap == CBC_MAX && voxels > 0 && n_lines > 0;
+    if (e == cudaSuccess && maxw)
+        e = cudaMemsetAsync(winner, 0x7f, sizeof(int) * (size_t)voxels, s);   /* no winner */
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    if (n_lines == 0) return CBC_OK;
+    if (voxels > 0) {
+        Rec3<T> *recs = reinterpret_cast<Rec3<T> *>(ws + L.recs);
+        Ck3<T> *cks = reinterpret_cast<Ck3<T> *>(ws + L.cks);
+        Vol v{(int)D, (int)H, (int)W};
+        const unsigned nb = (unsigned)((n_lines + kThreads - 1) / kThreads);
+        if (idxs && idx_bytes == 8)
+            prep3_kernel<T, int64_t><<<nb, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, v,
+                                                             recs, cks, ck_capacity, st);
+        else
+            prep3_kernel<T, int32_t><<<nb, kThreads, 0, s>>>(lines, idxs, n_lines, n_frames, v,
+                                                             recs, cks, ck_capacity, st);
+        note_launches(1);
+        Adj3Args<T> a{recs, cks, lines, v, st, gacc, max_val};
+        switch (kernel) {
+        case CBC_BIWEIGHT:    e = launch_adjoint3<T, CBC_BIWEIGHT>(a, overlap, grad_out, image, out0, winner, s); break;
+        case CBC_GAUSSIAN:    e = launch_adjoint3<T, CBC_GAUSSIAN>(a, overlap, grad_out, image, out0, winner, s); break;
+        case CBC_PARABOLIC:   e = launch_adjoint3<T, CBC_PARABOLIC>(a, overlap, grad_out, image, out0, winner, s); break;
+        case CBC_RECTANGULAR: e = launch_adjoint3<T, CBC_RECTANGULAR>(a, overlap, grad_out, image, out0, winner, s); break;
+        default:              e = launch_adjoint3<T, CBC_TRIANGULAR>(a, overlap, grad_out, image, out0, winner, s); break;
+        }
+        if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const long long n7 = 7 * n_lines;
+    const long long work = maxw && voxels > n7 ? voxels : n7;
+    long long blocks = (work + kThreads - 1) / kThreads;
+    if (blocks > 4096) blocks = 4096;
+    adjoint3_finish_kernel<T><<<(unsigned)blocks, kThreads, 0, s>>>(gacc, grad_lines, n7,
+                                                                    maxw ? winner : nullptr,
+                                                                    voxels);
+    note_launches(1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CBC_ERR_CUDA, cudaGetErrorString(e));
+    return CBC_OK;
+}
+
 }  // namespace l3
 }  // namespace cbc
 
@@ -1147,6 +1494,41 @@ int cbc_accumulate_lines_3d_f64(double *out, int64_t n_frames, int64_t depth, in
                                              max_val, kernel, in_overlap, out_overlap, workspace,
                                              workspace_bytes, checkpoint_capacity,
                                              table_capacity, stream);
+}
+
+size_t cbc_draw_lines_3d_backward_workspace_size(int64_t n_lines, int64_t checkpoint_capacity,
+                                                 int32_t elem_bytes)
+{
+    if (n_lines < 0 || checkpoint_capacity < 0 || (elem_bytes != 4 && elem_bytes != 8)) return 0;
+    return cbc::l3::adjoint3_workspace(n_lines, checkpoint_capacity, (size_t)elem_bytes);
+}
+
+int cbc_draw_lines_3d_backward_f32(const float *grad_out, int64_t n_frames, int64_t depth,
+                                   int64_t height, int64_t width, const float *lines,
+                                   int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                   float max_val, int32_t kernel, int32_t overlap,
+                                   const float *image, const float *out0, int32_t *winner,
+                                   float *grad_lines, void *workspace, size_t workspace_bytes,
+                                   int64_t checkpoint_capacity, void *stream)
+{
+    return cbc::l3::backward3_impl<float>(grad_out, n_frames, depth, height, width, lines,
+                                          n_lines, idxs, idx_bytes, max_val, kernel, overlap,
+                                          image, out0, winner, grad_lines, workspace,
+                                          workspace_bytes, checkpoint_capacity, stream);
+}
+
+int cbc_draw_lines_3d_backward_f64(const double *grad_out, int64_t n_frames, int64_t depth,
+                                   int64_t height, int64_t width, const double *lines,
+                                   int64_t n_lines, const void *idxs, int32_t idx_bytes,
+                                   double max_val, int32_t kernel, int32_t overlap,
+                                   const double *image, const double *out0, int32_t *winner,
+                                   double *grad_lines, void *workspace, size_t workspace_bytes,
+                                   int64_t checkpoint_capacity, void *stream)
+{
+    return cbc::l3::backward3_impl<double>(grad_out, n_frames, depth, height, width, lines,
+                                           n_lines, idxs, idx_bytes, max_val, kernel, overlap,
+                                           image, out0, winner, grad_lines, workspace,
+                                           workspace_bytes, checkpoint_capacity, stream);
 }
 
 }  // extern "C"

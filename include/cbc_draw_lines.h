@@ -462,6 +462,39 @@ CBC_API int cbc_accumulate_lines_3d_f64(double *out, int64_t n_frames, int64_t d
                                         int64_t checkpoint_capacity, int64_t table_capacity,
                                         void *stream);
 
+/* Adjoint of cbc_draw_lines_3d_* (no counterpart in the reference): grad_lines
+ * (n_lines, 7) = the gradient of sum(grad_out * volumes) with respect to
+ * (x0, y0, z0, x1, y1, z1, width), over exactly the voxel visits of the forward (a
+ * voxel the walk visits twice counts twice under sum overlap, as its value does).
+ * Max overlap gives each voxel's gradient to its winner only, the smallest line whose
+ * value equals `image` (the forward's result) and exceeds `out0` (the volumes before
+ * drawing; NULL: zeros); `winner` (n_frames, depth, height, width) int32 comes back
+ * holding those winners (0x7f7f7f7f where no line drew the value).  Workspace from
+ * cbc_draw_lines_3d_backward_workspace_size; capacity and errors as the forward. */
+CBC_API size_t cbc_draw_lines_3d_backward_workspace_size(int64_t n_lines,
+                                                         int64_t checkpoint_capacity,
+                                                         int32_t elem_bytes);
+
+CBC_API int cbc_draw_lines_3d_backward_f32(const float *grad_out, int64_t n_frames,
+                                           int64_t depth, int64_t height, int64_t width,
+                                           const float *lines, int64_t n_lines,
+                                           const void *idxs, int32_t idx_bytes, float max_val,
+                                           int32_t kernel, int32_t overlap, const float *image,
+                                           const float *out0, int32_t *winner,
+                                           float *grad_lines, void *workspace,
+                                           size_t workspace_bytes, int64_t checkpoint_capacity,
+                                           void *stream);
+
+CBC_API int cbc_draw_lines_3d_backward_f64(const double *grad_out, int64_t n_frames,
+                                           int64_t depth, int64_t height, int64_t width,
+                                           const double *lines, int64_t n_lines,
+                                           const void *idxs, int32_t idx_bytes,
+                                           double max_val, int32_t kernel, int32_t overlap,
+                                           const double *image, const double *out0,
+                                           int32_t *winner, double *grad_lines,
+                                           void *workspace, size_t workspace_bytes,
+                                           int64_t checkpoint_capacity, void *stream);
+
 /* Wait for `stream` and copy the device status of the last call that used
  * `workspace` into *status.  Returns CBC_OK or CBC_ERR_CUDA. */
 CBC_API int cbc_read_status(const void *workspace, cbc_status *status, void *stream);
