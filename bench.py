@@ -637,6 +637,8 @@ def run_accumulate(args, world, rank, local):
         cb = {'value': sub.n_lines / sec / 1e6, 'unit': 'Mlines/s', 'cores': threads,
               'kind': 'port',
               'sample': f'{k} of {ts.shape[0]} frames ({sub.n_lines} lines), one run'}
+    adj3 = _draw3d_adjoint_times(ts, lines, terms, frames, dev) \
+        if args.workload == 'rotomap' else None
     if rank == 0:
         print(json.dumps({
             'metric': 'accumulate_lines throughput', 'value': world * ts.n_lines / ms / 1e3,
@@ -647,7 +649,43 @@ def run_accumulate(args, world, rank, local):
                        'terms': int(ts.frames.size), 'kernel': ts.kernel,
                        'in_overlap': ts.in_overlap, 'out_overlap': ts.out_overlap,
                        'out': 'accumulated in place, not re-zeroed between steps'},
-            'clocks': clocks, 'gpu_launches': prof.launches, 'cpu_baseline': cb}), flush=True)
+            'clocks': clocks, 'gpu_launches': prof.launches, 'cpu_baseline': cb,
+            'draw3d_adjoint': adj3}), flush=True)
+
+
+def _draw3d_adjoint_times(ts, lines, terms, frames, dev):
+    """the workload's 3-D lines drawn with draw_lines into their volumes, and the
+    adjoint of that draw (gradient of sum(g * volumes) for a random g), sum and max
+    overlap: ms per call, CUDA events over 20 calls after 3 warm-up calls"""
+    import torch
+    from cbclib_v2_gb300 import autograd, draw_lines
+    idxs = frames.long()[terms.long()]
+    vol = torch.zeros(ts.shape, dtype=torch.float32, device=dev)
+    g = torch.rand(ts.shape, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, n=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    res = {'kernel': ts.kernel, 'lines': ts.n_lines}
+    for ov in ('sum', 'max'):
+        vol.zero_()
+        draw_lines(vol, lines, idxs, ts.max_val, ts.kernel, ov)
+        image = vol.clone()
+        res[ov] = {
+            'forward_ms': timed(lambda: draw_lines(vol, lines, idxs, ts.max_val, ts.kernel, ov)),
+            'adjoint_ms': timed(lambda: autograd.lines_backward(
+                g, lines, idxs, ts.max_val, ts.kernel, ov, image=image if ov == 'max' else None))}
+    return res
 
 
 def run_f64(args, world, rank, local):
