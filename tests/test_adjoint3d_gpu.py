@@ -154,3 +154,33 @@ def test_winners3d_and_out0_gradient(cuda):
     free = torch.tensor(w == _native.NO_WINNER, device='cuda')
     assert torch.equal(base.grad, torch.where(free, g, torch.zeros_like(g)))
     assert torch.all(ln.grad.abs().sum(1) > 0)
+
+
+def test_gradient3d_index_forms_and_errors(cuda):
+    """int32 and int64 frame indices give the same gradient; no indices draws line i
+    into volume i; an index beyond the volumes raises IndexError as the forward does"""
+    rng = np.random.default_rng(55)
+    lines = random_lines(rng, 5)
+    g = torch.tensor(rng.random(SHAPE), device='cuda')
+    ln = torch.tensor(lines, device='cuda')
+    i32 = torch.tensor(rng.integers(0, SHAPE[0], 5), dtype=torch.int32, device='cuda')
+    for overlap in ('sum', 'max'):
+        img = torch.zeros(SHAPE, dtype=torch.float64, device='cuda')
+        draw_lines(img, ln, i32, 1.2, 'biweight', overlap)
+        image = img if overlap == 'max' else None
+        a = autograd.lines_backward(g, ln, i32, 1.2, 'biweight', overlap, image=image)
+        b = autograd.lines_backward(g, ln, i32.long(), 1.2, 'biweight', overlap, image=image)
+        # the per-line sums are double atomics, added in any order
+        torch.testing.assert_close(a, b, rtol=1e-12, atol=1e-12)
+        assert bool(a.abs().sum() > 0)
+    per_line = (5,) + SHAPE[1:]
+    g5 = torch.tensor(rng.random(per_line), device='cuda')
+    img = torch.zeros(per_line, dtype=torch.float64, device='cuda')
+    draw_lines(img, ln, None, 1.2, 'biweight', 'sum')
+    none = autograd.lines_backward(g5, ln, None, 1.2, 'biweight', 'sum')
+    each = autograd.lines_backward(g5, ln, torch.arange(5, device='cuda'), 1.2, 'biweight', 'sum')
+    torch.testing.assert_close(none, each, rtol=1e-12, atol=1e-12)
+    bad = i32.clone()
+    bad[2] = SHAPE[0]
+    with pytest.raises(IndexError):
+        autograd.lines_backward(g, ln, bad, 1.2, 'biweight', 'sum')
