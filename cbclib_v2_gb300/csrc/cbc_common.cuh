@@ -865,6 +865,38 @@ struct PixelRing {
     unsigned char slot[kRing];     /* owner lane of each pixel */
 };
 
+/* Comparisons of the segment driver.  For double they compare bit patterns on the
+ * integer pipe (the float64 render is bound by the FP64 pipe): for doubles that are
+ * not NaN the signed order of the patterns of non-negative values is their order, and
+ * a negative pattern is a negative value or -0.  The walk's errors, the span
+ * threshold (>= 0) and the pixel errors (>= 0) are never NaN. */
+template <typename T>
+__device__ __forceinline__ bool abs_lt(T v, T thr) { return fabs(v) < thr; }
+template <>
+__device__ __forceinline__ bool abs_lt<double>(double v, double thr)
+{
+    return (__double_as_longlong(v) & 0x7fffffffffffffffll) < __double_as_longlong(thr);
+}
+
+/* t < 0 || t > hi, for hi >= 0 */
+template <typename T>
+__device__ __forceinline__ bool outside(T t, T hi) { return t < T(0) || t > hi; }
+template <>
+__device__ __forceinline__ bool outside<double>(double t, double hi)
+{
+    const long long b = __double_as_longlong(t);
+    return (b < 0 && b != LLONG_MIN) || b > __double_as_longlong(hi);
+}
+
+/* E <= 1 for an error E >= 0 */
+template <typename T>
+__device__ __forceinline__ bool le_one(T e) { return e <= T(1); }
+template <>
+__device__ __forceinline__ bool le_one<double>(double e)
+{
+    return __double_as_longlong(e) <= 0x3ff0000000000000ll;
+}
+
 /* an end-cap pixel (te < 0 or te > len^2) whose error is surely above 1: the error
  * E = (ta^2 + ne^2) / (len^2 w^2) in exact arithmetic, with ta = max(-te, te - len^2),
  * and the reference's float evaluation of E is within a few ulp of it, so
@@ -874,8 +906,12 @@ struct PixelRing {
 template <typename T>
 __device__ __forceinline__ bool cap_far(T te, T ne, T len2, T lim)
 {
-    const T ta = fmax(-te, te - len2);
-    return ta * ta + ne * ne > lim;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        return false;   /* four FP64 operations per span step cost the float64 render more */
+    } else {
+        const T ta = fmax(-te, te - len2);
+        return ta * ta + ne * ne > lim;
+    }
 }
 
 /* actions that draw only some lines define keep_line(line) */
@@ -968,7 +1004,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                     if (cap) p.len2 = S.len2[slot];
                     const T nf = A::nterm(v.ne, p);
                     const T E = cap ? A::error(v.te, nf, p) : A::error_inside(nf, p);
-                    if (E <= T(1)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne, pre);
+                    if (le_one(E)) act.pixel(S, slot, v.x, v.y, E, v.te, v.ne, pre);
                 } else {
                     /* the action decides from its own data which visited pixels count
                      * (the max-overlap adjoint: the pixel's winner) */
@@ -1070,7 +1106,7 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
             if (!col) cols = false;
 
             /* level 0: the column's centre pixel */
-            const bool cap_c = te_c < T(0) || te_c > len2;
+            const bool cap_c = outside(te_c, len2);
             push(col && sc >= 0 && sc <= s_hi && !(cap_c && cap_far(te_c, ne_c, len2, cap_lim)),
                  cap_c, te_c, ne_c, ax ? sc : c, ax ? c : sc);
             drain(31);
@@ -1084,10 +1120,10 @@ __device__ __forceinline__ void drive_segments(const DriveArgs<T> &a, Act &act)
                 td = A::sub(td, ts);
                 nd = A::sub(nd, ns);
                 const int su = sc + k, sd = sc - k;
-                up = up && fabs(nu) < thr && su <= s_hi;
-                dn = dn && fabs(nd) < thr && sd >= 0;
+                up = up && abs_lt(nu, thr) && su <= s_hi;
+                dn = dn && abs_lt(nd, thr) && sd >= 0;
                 if (!__any_sync(0xffffffffu, up || dn)) break;
-                const bool cap_u = tu < T(0) || tu > len2, cap_d = td < T(0) || td > len2;
+                const bool cap_u = outside(tu, len2), cap_d = outside(td, len2);
                 push2(up && su >= 0 && !(cap_u && cap_far(tu, nu, len2, cap_lim)), cap_u, tu, nu,
                       ax ? su : c, ax ? c : su,
                       dn && sd <= s_hi && !(cap_d && cap_far(td, nd, len2, cap_lim)), cap_d, td,
