@@ -383,10 +383,21 @@ struct Walker {
         n.exx = A::add(ne, d0n);
         n.eyy = A::add(ne, d1n);
         n.exy = A::add(n.exx, d1n);
-        const T axx = fabs(n.exx), ayy = fabs(n.eyy), axy = fabs(n.exy);
-        const bool ylt = ayy < axx;
-        n.nx = !ylt || axy < ayy;
-        n.ny = ylt || axy < axx;
+        if constexpr (sizeof(T) == sizeof(double)) {
+            /* |a| < |b| as the order of the sign-cleared bit patterns (integer pipe) */
+            constexpr long long m = 0x7fffffffffffffffll;
+            const long long axx = __double_as_longlong(n.exx) & m;
+            const long long ayy = __double_as_longlong(n.eyy) & m;
+            const long long axy = __double_as_longlong(n.exy) & m;
+            const bool ylt = ayy < axx;
+            n.nx = !ylt || axy < ayy;
+            n.ny = ylt || axy < axx;
+        } else {
+            const T axx = fabs(n.exx), ayy = fabs(n.eyy), axy = fabs(n.exy);
+            const bool ylt = ayy < axx;
+            n.nx = !ylt || axy < ayy;
+            n.ny = ylt || axy < axx;
+        }
         return n;
     }
     /* take the move: te gains d0t then d1t, ne becomes the move's candidate; written
