@@ -23,6 +23,25 @@ _ws_lock = threading.Lock()
 _workspaces = {}
 
 
+def _frames_arg(name: str, t: Optional[torch.Tensor], shape, dtype, dev) -> Optional[torch.Tensor]:
+    """`t` as a contiguous `dtype` tensor on `dev` with the frames' number of elements"""
+    if t is None:
+        return None
+    want = math.prod(int(x) for x in shape)
+    if t.numel() != want:
+        raise ValueError(f"{name} has {t.numel()} elements, the frames {tuple(shape)} have {want}")
+    return t.to(device=dev, dtype=dtype).contiguous()
+
+
+def _check_winner(winner: torch.Tensor, shape, dev) -> None:
+    """the winner buffer is written by the kernels: an int32 contiguous CUDA tensor on
+    the frames' device with one entry per pixel"""
+    want = math.prod(int(x) for x in shape)
+    if not (isinstance(winner, torch.Tensor) and winner.dtype == torch.int32 and
+            winner.is_contiguous() and winner.numel() == want and winner.device == dev):
+        raise ValueError(f"winner must be a contiguous int32 tensor of {want} elements on {dev}")
+
+
 def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dtype, dev,
               grad_out: Optional[torch.Tensor] = None, image: Optional[torch.Tensor] = None,
               out0: Optional[torch.Tensor] = None, winner: Optional[torch.Tensor] = None,
@@ -33,6 +52,13 @@ def _backward(lines, idxs, max_val: float, kernel: str, overlap: str, shape, dty
     k, ov = ndimage._check_names(kernel, overlap)
     if dtype not in (torch.float32, torch.float64):
         raise TypeError(f"frames must be float32 or float64, got {dtype}")
+    # every frame-shaped argument covers the frames, so no kernel reads or writes past it
+    grad_out = _frames_arg('grad_out', grad_out, shape, dtype, dev)
+    image = _frames_arg('image', image, shape, dtype, dev)
+    out0 = _frames_arg('out0', out0, shape, dtype, dev)
+    target = _frames_arg('target', target, shape, dtype, dev)
+    if winner is not None:
+        _check_winner(winner, shape, dev)
     ln = ndimage._as_device_lines(lines, dev, dtype)
     if ln.shape[1] == 7:
         if grad_out is None or packed is not None or winner_known:

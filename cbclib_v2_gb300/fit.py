@@ -85,8 +85,9 @@ def _sum_loss_step(image: torch.Tensor, target: torch.Tensor, lines, idxs, max_v
     k, _ = ndimage._check_names(kernel, 'sum')
     dev = target.device
     F, H, W = ndimage._frames_of(target)
-    if tuple(image.shape) != tuple(target.shape) or not image.is_contiguous():
-        raise ValueError("image must be a contiguous tensor of the target's shape")
+    if tuple(image.shape) != tuple(target.shape) or not image.is_contiguous() or \
+            image.device != target.device:
+        raise ValueError("image must be a contiguous tensor of the target's shape and device")
     ln = ndimage._as_device_lines(lines, dev, torch.float32)
     if ln.shape[1] != 5:
         raise ValueError("the fused loss step takes 2-D lines (N, 5)")

@@ -428,6 +428,11 @@ def draw_lines_max_winner(out: torch.Tensor, lines, idxs=None, max_val: float = 
         raise TypeError("out must be a float32 CUDA tensor")
     if winner is None:
         winner = torch.empty(out.shape, dtype=torch.int32, device=out.device)
+    elif not (isinstance(winner, torch.Tensor) and winner.dtype == torch.int32 and
+              winner.is_contiguous() and winner.numel() == out.numel() and
+              winner.device == out.device):
+        raise ValueError("winner must be a contiguous int32 tensor with one entry per pixel "
+                         "of out, on out's device")
     work = out if out.is_contiguous() else torch.empty(out.shape, dtype=out.dtype,
                                                        device=out.device)
     _max_winner(work, winner, out.shape, out.device, lines, idxs, max_val, kernel)
