@@ -10,9 +10,17 @@
  * --fmad=false, so every rounding matches the reference; the reference's
  * double-rounded steps go through exact.cuh.
  *
- * Pipeline (one stream, no host synchronisation):
+ * Lines strategy (the default; one stream, no host synchronisation):
  *   1. prep_kernel   one thread per line: frame index check, walk parameters
- *                    (LineRec), conservative tile coverage -> per-bin counts.
+ *                    (LineRec), checkpoint block, the list of long walks.
+ *   2. walk_ordered_kernel  one thread per line, long walks first: the exact walk
+ *                    state every 16 in-frame columns (walk checkpoints).
+ *   3. segments_kernel  persistent: warps take 32 (line, 8-column segment) items,
+ *                    replay the walks from their checkpoints, queue the visited
+ *                    pixels in per-warp rings and evaluate them on full warps, one
+ *                    L2 reduction per drawn pixel (drive_segments, cbc_common.cuh).
+ * Tiles strategy (on request):
+ *   1. prep_kernel   as above, plus conservative tile coverage -> per-bin counts.
  *   2. offsets_kernel  block scan of the per-bin counts, one atomic per block ->
  *                    bin offsets into the pair buffer (a counting sort on the
  *                    (frame, tile) key), capacity check.
@@ -22,6 +30,9 @@
  *                    (one thread per line), then evaluate the spans of all
  *                    (line, column) entries in parallel with shared-memory atomics,
  *                    write the tile back once.  Empty bins are never touched.
+ * Host frames (cbc_draw_lines_host_*): the lines strategy into a device scratch at
+ * the overlap's identity, then combine_host_kernel merges the drawn pixels into the
+ * host frames over NVLink-C2C.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
