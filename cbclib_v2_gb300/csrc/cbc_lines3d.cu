@@ -24,7 +24,9 @@
  * the column's checkpoint and combines each drawn voxel into `out` (sum: L2 add; max:
  * std::max merge; accumulate_lines with equal overlaps as in the 2-D path).
  * accumulate_lines with mixed overlaps builds each term in shared memory
- * (term_render3_kernel below).
+ * (term_render3_kernel below).  The adjoint (cbc_draw_lines_3d_backward_*) replays the
+ * same (column, quadrant) items with emitters that add each drawn voxel's gradient
+ * term to its line (winner pass first for max overlap; adjoint3_kernel below).
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
